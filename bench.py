@@ -1,0 +1,432 @@
+"""Benchmark of the fused lattice-Boltzmann step on GB300.
+
+Workload (default): D3Q19 BGK, FP32, 256^3 lattice, tau = 0.6, periodic on all
+six faces (NATIVE semantics), initialized at equilibrium from
+rho = 1 + 1e-3 N(0,1) and a Taylor-Green velocity field of amplitude 0.02 plus
+1e-4 N(0,1) per component (seed 20261203).  A step is one time step of the
+whole lattice; the metric is MLUPS (lattice cell updates per microsecond).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One JSON line is printed by rank 0.  Under torchrun every rank advances its
+own replica of the workload on its own GPU (the time step has no data-parallel
+split that needs an exchange: replicas only), the timed region is bracketed by
+barriers, and the slowest rank's time is used.
+
+  value      MLUPS of K fused steps with the state resident in HBM (CUDA events
+             on the solve's stream); the populations (2.7 GB) are larger than
+             L2, so no flush is needed between steps.
+  e2e        MLUPS through the C ABI with host buffers: upload n, rho, u from
+             pinned memory (plbpd's layout), march K steps, read rho and u back.
+  roofline   achieved = 152 B/cell (19 populations read and written, FP32) x
+             cells / mean duration of one fused-kernel launch, against the
+             measured HBM copy bandwidth.
+  cpu_baseline  the CPU oracle (or the reference itself where it was compiled)
+             on the host cores, on a bounded sample of the workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SEED = 20261203
+N_SIDE = 256
+Q = 19
+BYTES_PER_CELL = 2 * Q * 4          # one read and one write of every FP32 population
+TAU = 0.6
+PERIODIC = {f: "periodic" for f in ("east", "west", "north", "south", "up", "down")}
+WORKLOAD = "D3Q19 BGK 256^3, tau 0.6, fully periodic, Taylor-Green A=0.02 + noise, FP32"
+
+
+def nu_for_tau(tau: float) -> float:
+    """A float viscosity whose float tau = 3 nu + 0.5 equals float(tau)."""
+    target = np.float32(tau)
+    nu = np.float32((tau - 0.5) / 3.0)
+    for _ in range(64):
+        t = np.float32(np.float32(3.0) * nu) + np.float32(0.5)
+        if t == target:
+            return float(nu)
+        nu = np.nextafter(nu, np.float32(np.inf) if t < target else np.float32(-np.inf))
+    return float(nu)
+
+
+# ---------------------------------------------------------------------------
+# initial state (host, plbpd's layout)
+# ---------------------------------------------------------------------------
+def lattice(q=Q):
+    from plbpd_gb300 import capi
+    c, w, _, _ = capi.model_tables({9: "D2Q9", 19: "D3Q19", 27: "D3Q27"}[q])
+    return c, w
+
+
+def taylor_green_state(n_side: int, out_n=None, out_rho=None, out_u=None):
+    """rho, u and EqlbDist(rho, u) (src/EqlbDist.hpp:26-38 rounding) on the
+    interior of plbpd-layout arrays (nz+2, ny+2, nx+2, V)."""
+    rng = np.random.default_rng(SEED)
+    N = n_side
+    shape3 = (N, N, N)
+    rho = (1.0 + 1e-3 * rng.standard_normal(shape3)).astype(np.float32)
+    ax = 2.0 * np.pi * np.arange(N) / N
+    zc, yc, xc = np.meshgrid(ax, ax, ax, indexing="ij")
+    A = 0.02
+    ux = (A * np.sin(xc) * np.cos(yc) * np.cos(zc) + 1e-4 * rng.standard_normal(shape3)).astype(np.float32)
+    uy = (-A * np.cos(xc) * np.sin(yc) * np.cos(zc) + 1e-4 * rng.standard_normal(shape3)).astype(np.float32)
+    uz = (1e-4 * rng.standard_normal(shape3)).astype(np.float32)
+    del zc, yc, xc
+    full = (N + 2, N + 2, N + 2)
+    n_arr = out_n if out_n is not None else np.zeros(full + (Q,), np.float32)
+    r_arr = out_rho if out_rho is not None else np.zeros(full + (1,), np.float32)
+    u_arr = out_u if out_u is not None else np.zeros(full + (3,), np.float32)
+    r_arr[1:-1, 1:-1, 1:-1, 0] = rho
+    u_arr[1:-1, 1:-1, 1:-1, 0] = ux
+    u_arr[1:-1, 1:-1, 1:-1, 1] = uy
+    u_arr[1:-1, 1:-1, 1:-1, 2] = uz
+    c, w = lattice()
+    usq = (ux * ux + uy * uy) + uz * uz
+    for k in range(Q):
+        cu = (np.float32(c[k, 0]) * ux + np.float32(c[k, 1]) * uy) + np.float32(c[k, 2]) * uz
+        wr = (w[k] * rho).astype(np.float64)
+        cud = cu.astype(np.float64)
+        br = 1.0 + 3.0 * cud + 4.5 * cud * cud - 1.5 * usq.astype(np.float64)
+        n_arr[1:-1, 1:-1, 1:-1, k] = (wr * br).astype(np.float32)
+    return n_arr, r_arr, u_arr
+
+
+# ---------------------------------------------------------------------------
+# clocks during a timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self._t.join(timeout=2)
+
+    def summary(self):
+        rows = []
+        for l in self.lines:
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                rows.append((float(parts[0]), float(parts[1]), float(parts[2]), parts[4:8]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower().startswith("active")})
+        loaded = [r for r in rows if r[2] > 200.0] or rows
+        return {"sm_mhz": float(np.median([r[0] for r in loaded])), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(r[2] for r in rows)}
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers (torchrun: one process per GPU)
+# ---------------------------------------------------------------------------
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def dist_init(world: int, backend: str):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        dist.init_process_group(backend=backend)
+    return dist
+
+
+def barrier(dist, device=None):
+    if dist is not None:
+        if device is not None:
+            dist.barrier(device_ids=[device])
+        else:
+            dist.barrier()
+
+
+def aggregate(dist, local_ms: float, local_units: float, device=None):
+    """Slowest rank's time and the units of all ranks."""
+    if dist is None:
+        return local_ms, local_units
+    import torch
+    dev = torch.device("cuda", device) if device is not None else torch.device("cpu")
+    t = torch.tensor([local_ms], dtype=torch.float64, device=dev)
+    u = torch.tensor([local_units], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (oracle port, or the reference compiled in oracle/_ref)
+# ---------------------------------------------------------------------------
+def cpu_baseline(seconds: float = 12.0, slab: int | None = None):
+    """MLUPS of the CPU implementation on the host cores.  The reference
+    itself when it was compiled here (it cannot express z-periodicity, so it
+    runs the nearest setup it can: x/y periodic, resting z walls), else the
+    oracle port on the same fully periodic workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    threads = os.cpu_count() or 1
+    nz = slab or N_SIDE
+    nu = nu_for_tau(TAU)
+    if po.ref_available("omp"):
+        sim = po.RefSim("D3Q19", N_SIDE, N_SIDE, nz, nu, 1.0, (0, 0, 0), (0, 0, 0), 1.0,
+                        {"east": "periodic", "west": "periodic", "north": "periodic", "south": "periodic",
+                         "up": "noslip", "down": "noslip"}, {"up": (0, 0, 0), "down": (0, 0, 0)},
+                        variant="omp", threads=threads)
+        kind = "reference"
+        setup = "x/y periodic, z walls (the reference has no z-periodicity)"
+    else:
+        sim = po.Port("D3Q19", N_SIDE, N_SIDE, nz, nu, 1.0, (0, 0, 0), (0, 0, 0), 1.0, PERIODIC, {},
+                      mode=po.MODE_NATIVE, arith=po.ARITH_AVX2, threads=threads)
+        kind = "port"
+        setup = "fully periodic (oracle restatement of the reference's operator sequence)"
+    sim.initialize()
+    sim.step(1)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        sim.step(1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or (steps >= 3 and el >= 0.5 * seconds and el / steps > seconds / 4):
+            break
+    cells = N_SIDE * N_SIDE * nz
+    val = cells * steps / el / 1e6
+    return {"value": round(val, 2), "unit": "MLUPS", "cores": threads, "kind": kind,
+            "sample": f"D3Q19 {N_SIDE}x{N_SIDE}x{nz}, {steps} time steps, {setup}; {el:.1f} s"}
+
+
+def run_reference_arm(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    # each step: one time step of a 256x256x16 slab (the same per-cell work,
+    # sized so that K steps end within a few minutes)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    threads = os.cpu_count() or 1
+    nu = nu_for_tau(TAU)
+    slab = 16
+    if po.ref_available("omp"):
+        sim = po.RefSim("D3Q19", N_SIDE, N_SIDE, slab, nu, 1.0, (0, 0, 0), (0, 0, 0), 1.0,
+                        {"east": "periodic", "west": "periodic", "north": "periodic", "south": "periodic",
+                         "up": "noslip", "down": "noslip"}, {"up": (0, 0, 0), "down": (0, 0, 0)},
+                        variant="omp", threads=threads)
+        kind, setup = "reference", "the reference's PLBPD loop, x/y periodic, z walls"
+    else:
+        sim = po.Port("D3Q19", N_SIDE, N_SIDE, slab, nu, 1.0, (0, 0, 0), (0, 0, 0), 1.0, PERIODIC, {},
+                      mode=po.MODE_NATIVE, arith=po.ARITH_AVX2, threads=threads)
+        kind, setup = "port", "oracle restatement of the reference's operator sequence, fully periodic"
+    sim.initialize()
+    sim.step(max(args.warmup, 0))
+    t0 = time.perf_counter()
+    sim.step(args.steps)
+    el = time.perf_counter() - t0
+    cells = N_SIDE * N_SIDE * slab
+    val = cells * args.steps / el / 1e6
+    sample = f"D3Q19 {N_SIDE}x{N_SIDE}x{slab} slab per step, {args.steps} steps, {setup}"
+    line = {"impl": "reference", "metric": "MLUPS", "value": round(val, 2), "unit": "MLUPS", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(el * 1e3 / max(args.steps, 1), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "sample": f"{N_SIDE}x{N_SIDE}x{slab}"},
+            "cpu_baseline": {"value": round(val, 2), "unit": "MLUPS", "cores": threads, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": round(val, 2), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+def read_traffic():
+    """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "nat_fused_d3q19_256.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def run_gpu_arm(args):
+    world, rank, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    dist = dist_init(world, "nccl")
+    from plbpd_gb300 import capi
+
+    nu = nu_for_tau(TAU)
+    params = capi.make_params("D3Q19", N_SIDE, N_SIDE, N_SIDE, nu, rho0=1.0, face_type=PERIODIC,
+                              semantics=capi.SEMANTICS_NATIVE, arith=capi.ARITH_FP32,
+                              storage=capi.STORAGE_FP32, device=local)
+    cells = N_SIDE ** 3
+    full = (N_SIDE + 2,) * 3
+    pin_n = capi.PinnedBuffer(full + (Q,))
+    pin_rho = capi.PinnedBuffer(full + (1,))
+    pin_u = capi.PinnedBuffer(full + (3,))
+    out_rho = capi.PinnedBuffer(full + (1,))
+    out_u = capi.PinnedBuffer(full + (3,))
+    taylor_green_state(N_SIDE, pin_n.array, pin_rho.array, pin_u.array)
+
+    s = capi.Solve(params)
+    stream = torch.cuda.ExternalStream(s.stream(), device=torch.device("cuda", local))
+
+    def upload():
+        s.set(capi.FIELD_N, pin_n.array)
+        s.set(capi.FIELD_RHO, pin_rho.array)
+        s.set(capi.FIELD_U, pin_u.array)
+
+    upload()
+    s.step(args.warmup)                       # RAW -> steady fused steps
+    s.synchronize()
+
+    # ---- value: K fused steps, device resident --------------------------------
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(dist, local)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        s.step_async(args.steps)
+        e1.record(stream)
+        s.synchronize()
+        torch.cuda.synchronize()
+    barrier(dist, local)
+    local_ms = e0.elapsed_time(e1)
+    ms, units = aggregate(dist, local_ms, float(cells) * args.steps, local)
+    value = units / (ms * 1e-3) / 1e6
+
+    # ---- mean duration of one fused-kernel launch -----------------------------
+    launches = 20
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(launches)]
+    for a, b in evs:
+        a.record(stream)
+        s.step_async(1)
+        b.record(stream)
+    s.synchronize()
+    kms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+
+    # ---- e2e through the C ABI with host buffers -------------------------------
+    e2e_iters = max(1, args.e2e_iters)
+    barrier(dist, local)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk2:
+        t0 = time.perf_counter()
+        for _ in range(e2e_iters):
+            upload()
+            s.step(args.steps)
+            s.get(capi.FIELD_RHO, out_rho.array)
+            s.get(capi.FIELD_U, out_u.array)
+        t1 = time.perf_counter()
+    barrier(dist, local)
+    e2e_ms, e2e_units = aggregate(dist, (t1 - t0) * 1e3, float(cells) * args.steps * e2e_iters, local)
+    e2e_val = e2e_units / (e2e_ms * 1e-3) / 1e6
+    h2d = (pin_n.nbytes + pin_rho.nbytes + pin_u.nbytes) / args.steps
+    d2h = (out_rho.nbytes + out_u.nbytes) / args.steps
+    mass = s.conservation()[0]
+    s.close()
+
+    if rank != 0:
+        return 0
+    peak, peak_kind = measured_peak()
+    achieved = BYTES_PER_CELL * cells / (kms * 1e-3) / 1e9
+    traffic = read_traffic()
+    cs = clk.summary() or clk2.summary()
+    line = {
+        "metric": "MLUPS", "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "lattice": "D3Q19", "cells": cells, "tau": TAU,
+                   "boundaries": "periodic x/y/z", "storage": "fp32", "semantics": "native",
+                   "l2": "no flush: populations 2.7 GB > 129 MB L2", "parallelism": f"replicas x{world}",
+                   "e2e": f"{e2e_iters} x (upload n/rho/u, {args.steps} steps, read rho/u)"},
+        "e2e": {"value": round(e2e_val, 1), "unit": "MLUPS", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                     "kernel": "nat_fused_k<19,fp32,nomask>", "bytes_per_cell": BYTES_PER_CELL,
+                     "kernel_ms": round(kms, 4)},
+        "gpu_launches": int(args.steps),
+        "clocks": cs,
+        "mass_after": mass,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--e2e-iters", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    return run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

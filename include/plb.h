@@ -1,0 +1,204 @@
+/*
+ * plb.h -- C ABI of the GB300 lattice-Boltzmann engine (libplb_gb300.so).
+ *
+ * One opaque handle (plb_solve) is one lattice-Boltzmann problem whose state
+ * lives in GPU memory.  Every entry point takes plain pointers and sizes,
+ * returns an int status (PLB_OK == 0, negative on error) and records a
+ * message readable with plb_last_error().  The C++ classes in
+ * include/plbpd/ (LBModel, Domain, Boundary, SimData, CollisionSRT, Streaming,
+ * CalcMoments, LBDynamics, PLBPD, Flow) sit on top of these calls and throw
+ * the exception types plbpd throws.
+ *
+ * Each declaration names the plbpd interface it replaces (paths inside the
+ * plbpd project).
+ *
+ * Coordinates, layouts and faces follow plbpd:
+ *   - domain sizes nx, ny, nz are plbpd's Domain(x, y, z) (src/Domain.cpp:13-22);
+ *   - host arrays use plbpd's Field layout (src/Field.hpp:37-47,91-93): AoS
+ *     with one halo layer on every axis, element ((z*(ny+2)+y)*(nx+2)+x)*V+v,
+ *     interior coordinates 1..n;
+ *   - faces are numbered east, west, north, south, up, down
+ *     (src/Boundary.cpp:17-18): east/west bound x, north/south bound y,
+ *     up/down bound z.
+ */
+#ifndef PLB_GB300_PLB_H_
+#define PLB_GB300_PLB_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define PLB_OK 0
+#define PLB_EINVAL (-1)       /* bad argument: plbpd throws logic_error / invalid_argument */
+#define PLB_ENOMEM (-2)       /* device or host allocation failed                       */
+#define PLB_ECUDA (-3)        /* a CUDA call failed                                      */
+#define PLB_ETIMEOUT (-4)     /* a bounded wait ran out                                  */
+#define PLB_ESTATE (-5)       /* call not valid in the handle's current state            */
+#define PLB_EUNSUPPORTED (-6) /* combination the engine does not implement               */
+
+/* ---- enumerations -------------------------------------------------------- */
+#define PLB_FACE_NONE 0
+#define PLB_FACE_PERIODIC 1
+#define PLB_FACE_NOSLIP 2
+
+#define PLB_FACE_EAST 0
+#define PLB_FACE_WEST 1
+#define PLB_FACE_NORTH 2
+#define PLB_FACE_SOUTH 3
+#define PLB_FACE_UP 4
+#define PLB_FACE_DOWN 5
+
+/* Boundary semantics.
+ * REFERENCE: plbpd's exact operator sequence -- halo-copy periodicity on
+ *   east/west and north/south only (src/Boundary.cpp:91-99,234-281), no-slip
+ *   on the wall layers in plbpd's serial order (src/Boundary.cpp:189-221),
+ *   push streaming into a double buffer (src/Streaming.cpp:62-94).  Results
+ *   reproduce plbpd bit for bit, seams included.  FP32 storage only.
+ * NATIVE: every periodic axis (z included) wraps around; every other face is
+ *   a no-slip wall layer; an optional obstacle mask adds solid nodes; one
+ *   fused pull kernel per step.  FP32 or FP16 storage.                      */
+#define PLB_SEMANTICS_REFERENCE 0
+#define PLB_SEMANTICS_NATIVE 1
+
+/* Collision arithmetic (src/CollisionSRT.cpp:93-148).
+ * REFERENCE: plbpd's AVX2 kernel op for op -- FP32 8-wide body, FP64 bracket
+ *   for the directions past the last multiple of 8 -- so populations match
+ *   plbpd's AVX2 build with -ffp-contract=off bit for bit.
+ * FP32: the FP32 body's sequence for every direction; no FP64 on the GPU.  */
+#define PLB_ARITH_REFERENCE 0
+#define PLB_ARITH_FP32 1
+
+/* Population storage.  FP16_DEV keeps f_k - w_k in IEEE half precision and
+ * does all collision arithmetic in FP32 (NATIVE semantics only).          */
+#define PLB_STORAGE_FP32 0
+#define PLB_STORAGE_FP16_DEV 1
+
+/* Field ids: plbpd's SimData members n, ntmp, rho, u (src/SimData.hpp:18-21). */
+#define PLB_FIELD_N 0
+#define PLB_FIELD_NTMP 1
+#define PLB_FIELD_RHO 2
+#define PLB_FIELD_U 3
+
+typedef struct plb_solve plb_solve;
+
+/* Problem description: plbpd's LBModel + Domain + Boundary constructor
+ * arguments in one struct.  Replaces
+ *   LBModel(std::string)                                   src/LBModel.hpp:25
+ *   Domain(lbmodel, x, y, z, nu, rho, u0, F)               src/Domain.hpp:23-28
+ *   Boundary(lbmodel, domain, rho_solid, types, velocities) src/Boundary.hpp:55-60 */
+typedef struct plb_params {
+    int32_t q;                  /* 9 (D2Q9), 19 (D3Q19) or 27 (D3Q27)              */
+    int64_t nx, ny, nz;         /* interior extents, each >= 1                      */
+    float nu;                   /* viscosity; tau = 3*nu + 0.5 in float             */
+    float rho0;                 /* initial density                                  */
+    float u0[3];                /* initial velocity                                 */
+    float force[3];             /* body force, applied as u + F*tau/rho             */
+    float rho_solid;            /* density written on no-slip faces                 */
+    int32_t face_type[6];       /* PLB_FACE_*, order east..down                     */
+    int32_t face_has_vel[6];    /* nonzero: face_vel[f] is given                    */
+    float face_vel[6][3];       /* wall velocity u_b per face                       */
+    int32_t semantics;          /* PLB_SEMANTICS_*                                  */
+    int32_t arith;              /* PLB_ARITH_*                                      */
+    int32_t storage;            /* PLB_STORAGE_*                                    */
+    int32_t device;             /* CUDA device ordinal                              */
+} plb_params;
+
+/* ---- library ----------------------------------------------------------- */
+/* Message of the last failed call on this thread ("" if none). */
+const char* plb_last_error(void);
+/* Library version, major*10000 + minor*100 + patch. */
+int plb_version(void);
+
+/* Lattice tables of a named model.  Replaces LBModel(name) and its getters
+ * (src/LBModel.cpp:8-19,167-189).  c: Q*3 int32, w: Q floats, rev: Q uint32.
+ * Returns Q, or PLB_EINVAL for an unknown name (plbpd: "Model X not yet
+ * implemented", src/LBModel.cpp:17).  Any output pointer may be NULL. */
+int plb_model_tables(const char* name, int32_t* c, float* w, uint32_t* rev, float* cs2);
+
+/* Equilibrium populations on one node.  Replaces EqlbDist::operator()
+ * (src/EqlbDist.hpp:26-38), same rounding: float usq and c.u, FP64 bracket. */
+int plb_equilibrium(int32_t q, float rho, const float* u3, float* out_q);
+
+/* tau and omega as CollisionSRT derives them (src/CollisionSRT.cpp:19-20). */
+int plb_relaxation(float nu, float* tau, float* omega);
+
+/* ---- solve lifetime ------------------------------------------------------ */
+/* Creates the solve and its device buffers.  Replaces constructing
+ * SimData(dims, Q) (src/SimData.cpp:22-30) together with the operator objects
+ * CollisionSRT, Streaming, CalcMoments, LBDynamics and PLBPD
+ * (src/PLBPD.cpp:6-14).  Fields start as plbpd's do: n, ntmp, rho, u = 0. */
+int plb_solve_create(const plb_params* params, plb_solve** out);
+int plb_solve_destroy(plb_solve* s);
+
+/* Obstacle mask, nz*ny*nx bytes with x fastest, nonzero = solid.  NATIVE
+ * semantics only (plbpd has no obstacle masks; its wall rule,
+ * src/Boundary.cpp:189-221, is applied to every solid node). */
+int plb_set_mask(plb_solve* s, const uint8_t* mask);
+
+/* Domain::initialize + Boundary::reset (src/PLBPD.cpp:16-19,
+ * src/Domain.cpp:46-63, src/Boundary.cpp:58-89): rho0, u0 and
+ * EqlbDist(rho0, u0) on every node, then the wall resets. */
+int plb_initialize(plb_solve* s);
+
+/* PLBPD::march_in_time (src/PLBPD.cpp:21-33): nsteps of collide, push,
+ * no-slip, periodic copy, moments, reset, fused.  Blocks until done. */
+int plb_step(plb_solve* s, int64_t nsteps);
+/* Same, enqueued on the solve's stream; returns without waiting. */
+int plb_step_async(plb_solve* s, int64_t nsteps);
+/* Waits for the solve's stream. */
+int plb_synchronize(plb_solve* s);
+/* The solve's CUDA stream (a cudaStream_t), for callers that order their own
+ * work after plb_step_async. */
+void* plb_stream_handle(plb_solve* s);
+
+/* ---- the unfused plbpd operators (REFERENCE semantics) ---------------------
+ * Each runs one operator of plbpd's loop on the device state, with plbpd's
+ * semantics, so the plbpd classes can be driven operator by operator.     */
+/* CollisionSRT::operator() (src/CollisionSRT.cpp:25-69): in place on n with
+ * the current rho and u fields. */
+int plb_collide(plb_solve* s);
+/* Streaming::operator()(simdata, "push") (src/Streaming.cpp:31-94): push into
+ * ntmp, then n and ntmp swap. */
+int plb_stream_push(plb_solve* s);
+/* Boundary::apply_noslip (src/Boundary.cpp:101-111,189-221). */
+int plb_apply_noslip(plb_solve* s);
+/* Boundary::apply_periodicity (src/Boundary.cpp:91-99,234-281). */
+int plb_apply_periodicity(plb_solve* s);
+/* CalcMoments::operator() (src/CalcMoments.hpp:47-73). */
+int plb_calc_moments(plb_solve* s);
+/* Boundary::reset (src/Boundary.cpp:58-66): reset_velocity then reset_density. */
+int plb_reset(plb_solve* s);
+/* Boundary::reset_velocity / reset_density (src/Boundary.cpp:68-89). */
+int plb_reset_velocity(plb_solve* s);
+int plb_reset_density(plb_solve* s);
+
+/* ---- state transfer (host buffers, plbpd's Field layout) ------------------
+ * Replaces reading/writing SimData's public Field pointers
+ * (src/SimData.hpp:18-21, Field::at/get src/Field.hpp:95-109).  `out`/`in`
+ * hold plb_field_len() floats.  Under NATIVE semantics the halo slots carry
+ * no state (read back as 0) and ntmp reads back as 0. */
+size_t plb_field_len(const plb_solve* s, int32_t which);
+int plb_get_field(plb_solve* s, int32_t which, float* out);
+int plb_set_field(plb_solve* s, int32_t which, const float* in);
+
+/* Sums over the fluid nodes of n_k (mass) and n_k c_k (momentum), in FP64 on
+ * the device: out[0] = mass, out[1..3] = momentum.  No plbpd counterpart;
+ * plbpd has no conservation diagnostics. */
+int plb_conservation(plb_solve* s, double* out4);
+
+/* Pinned host memory for fast transfers (cudaHostAlloc / cudaFreeHost). */
+int plb_host_alloc(size_t bytes, void** out);
+int plb_host_free(void* p);
+
+/* Device bytes the solve holds. */
+int64_t plb_device_bytes(const plb_solve* s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PLB_GB300_PLB_H_ */

@@ -1,0 +1,684 @@
+// The C ABI (include/plb.h): handle lifetime, validation, state tracking,
+// step orchestration (CUDA-graph chunks of fused steps) and transfers between
+// host buffers in plbpd's layout and the device layout.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "../../include/plb.h"
+#include "engine.h"
+
+using namespace plb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define PLB_CUDA(call)                                                                        \
+    do {                                                                                      \
+        const cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(PLB_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));      \
+    } while (0)
+
+#define PLB_KERNEL(call)                                                                      \
+    do {                                                                                      \
+        const int e_ = (call);                                                                \
+        if (e_ != 0)                                                                          \
+            return fail(PLB_ECUDA, std::string(#call) + ": " +                                \
+                                   cudaGetErrorString(static_cast<cudaError_t>(e_)));         \
+    } while (0)
+
+#define PLB_TRY(call)                 \
+    do {                              \
+        const int r_ = (call);        \
+        if (r_ != PLB_OK) return r_;  \
+    } while (0)
+
+// ---- host-side lattice tables (the same constexpr tables the kernels use) --
+template <int Q>
+void tables_of(int32_t* c, float* w, uint32_t* rev) {
+    for (int k = 0; k < Q; ++k) {
+        if (c) { c[3 * k] = Lattice<Q>::cx(k); c[3 * k + 1] = Lattice<Q>::cy(k); c[3 * k + 2] = Lattice<Q>::cz(k); }
+        if (w) w[k] = weight<Q>(k);
+        if (rev) rev[k] = (uint32_t)rev_of(k);
+    }
+}
+
+bool tables(int q, int32_t* c, float* w, uint32_t* rev) {
+    if (q == 9) tables_of<9>(c, w, rev);
+    else if (q == 19) tables_of<19>(c, w, rev);
+    else if (q == 27) tables_of<27>(c, w, rev);
+    else return false;
+    return true;
+}
+
+// EqlbDist::operator() (src/EqlbDist.hpp:26-38): float usq and c.u, the
+// bracket in double, times the float w*rho, rounded to float.
+void host_eqlb(int q, float rho, const float* u, float* out) {
+    int32_t c[27 * 3];
+    float w[27];
+    tables(q, c, w, nullptr);
+    const float usq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    for (int k = 0; k < q; ++k) {
+        const float cu = (float)c[3 * k] * u[0] + (float)c[3 * k + 1] * u[1] + (float)c[3 * k + 2] * u[2];
+        const float wr = w[k] * rho;
+        const double cud = (double)cu;
+        out[k] = (float)((double)wr * (1.0 + 3.0 * cud + 4.5 * cud * cud - 1.5 * (double)usq));
+    }
+}
+
+// CollisionSRT's constructor (src/CollisionSRT.cpp:19-20); this file is
+// compiled with -ffp-contract=off, so each operation rounds separately.
+void relaxation(float nu, float* tau, float* omega) {
+    const float three_nu = 3.0f * nu;
+    *tau = three_nu + 0.5f;
+    *omega = (float)(1. / (double)*tau);
+}
+
+long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
+
+int graph_steps_default() {
+    const char* e = std::getenv("PLB_GRAPH_STEPS");
+    if (!e) return 64;
+    int v = std::atoi(e);
+    if (v < 0) v = 0;
+    return v & ~1;   // even, so a chunk returns the buffers to their parity
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+struct plb_solve {
+    plb_params p;
+    int q = 0;
+    bool native = false;
+    int storage = 0;
+    Geo g{};
+    CollideParams cp{};
+    FaceParams fp{};
+    NativeParams np{};
+    cudaStream_t stream = nullptr;
+    void* f[2] = {nullptr, nullptr};
+    int cur = 0;
+    float* rho = nullptr;
+    float* u = nullptr;
+    float* consts = nullptr;     // 2q floats: equilibrium(rho0, u0), weights
+    uint8_t* types = nullptr;    // NATIVE node types
+    uint8_t* types_tmp = nullptr;
+    uint8_t* mask_dev = nullptr;
+    bool has_mask = false;       // NATIVE: walls or obstacles exist
+    float* staging = nullptr;    // plbpd-layout transfer buffer
+    size_t staging_len = 0;
+    double* partials = nullptr;
+    double* out4 = nullptr;
+    double* out4_host = nullptr;
+    // REFERENCE: rho/u fields hold what the next collision must use
+    bool fields_valid = true;
+    // NATIVE: false = RAW (buffer cur holds n), true = POST (holds P_{t-1})
+    bool post = false;
+    // no-slip launch groups (REFERENCE)
+    int groups[6][2];
+    int group_len[6];
+    int ngroups = 0;
+    int graph_steps = 64;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int64_t device_bytes = 0;
+};
+
+namespace {
+
+int set_device(const plb_solve* s) {
+    int cur = -1;
+    PLB_CUDA(cudaGetDevice(&cur));
+    if (cur != s->p.device) PLB_CUDA(cudaSetDevice(s->p.device));
+    return PLB_OK;
+}
+
+int dalloc(plb_solve* s, void** p, size_t bytes) {
+    const cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(PLB_ENOMEM, std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+    }
+    s->device_bytes += (int64_t)bytes;
+    return PLB_OK;
+}
+
+void drop_graphs(plb_solve* s) {
+    for (int i = 0; i < 2; ++i)
+        if (s->graph[i]) { cudaGraphExecDestroy(s->graph[i]); s->graph[i] = nullptr; }
+}
+
+void release(plb_solve* s) {
+    if (!s) return;
+    drop_graphs(s);
+    for (void* ptr : {s->f[0], s->f[1], (void*)s->rho, (void*)s->u, (void*)s->consts, (void*)s->types,
+                      (void*)s->types_tmp, (void*)s->mask_dev, (void*)s->staging, (void*)s->partials,
+                      (void*)s->out4})
+        if (ptr) cudaFree(ptr);
+    if (s->out4_host) cudaFreeHost(s->out4_host);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+int validate(const plb_params* p) {
+    if (!p) return fail(PLB_EINVAL, "params is null");
+    if (p->q != 9 && p->q != 19 && p->q != 27)
+        return fail(PLB_EINVAL, "Model with " + std::to_string(p->q) + " directions not yet implemented");
+    if (p->nx < 1 || p->ny < 1 || p->nz < 1) return fail(PLB_EINVAL, "argument is zero");
+    if (p->ny > 65535 || p->nz > 65535 || p->nx > (1ll << 30))
+        return fail(PLB_EINVAL, "domain extent too large (ny, nz <= 65535)");
+    for (int f = 0; f < 6; ++f) {
+        if (p->face_type[f] < PLB_FACE_NONE || p->face_type[f] > PLB_FACE_NOSLIP)
+            return fail(PLB_EINVAL, "invalid face type");
+        // src/Boundary.cpp:197 reads the velocity of every no-slip face
+        if (p->face_type[f] == PLB_FACE_NOSLIP && !p->face_has_vel[f])
+            return fail(PLB_EINVAL, "no-slip face " + std::to_string(f) + " has no velocity entry");
+    }
+    if (p->semantics != PLB_SEMANTICS_REFERENCE && p->semantics != PLB_SEMANTICS_NATIVE)
+        return fail(PLB_EINVAL, "invalid semantics");
+    if (p->arith != PLB_ARITH_REFERENCE && p->arith != PLB_ARITH_FP32) return fail(PLB_EINVAL, "invalid arith");
+    if (p->storage != PLB_STORAGE_FP32 && p->storage != PLB_STORAGE_FP16_DEV)
+        return fail(PLB_EINVAL, "invalid storage");
+    if (p->storage == PLB_STORAGE_FP16_DEV && p->semantics != PLB_SEMANTICS_NATIVE)
+        return fail(PLB_EUNSUPPORTED, "FP16 storage needs NATIVE semantics");
+    if (p->semantics == PLB_SEMANTICS_NATIVE) {
+        int32_t c[27 * 3];
+        tables(p->q, c, nullptr, nullptr);
+        for (int a = 0; a < 3; ++a) {
+            bool moves = false;
+            for (int k = 0; k < p->q; ++k) moves |= c[3 * k + a] != 0;
+            const int t0 = p->face_type[2 * a], t1 = p->face_type[2 * a + 1];
+            const bool per = t0 == PLB_FACE_PERIODIC && t1 == PLB_FACE_PERIODIC;
+            const bool wall = t0 == PLB_FACE_NOSLIP && t1 == PLB_FACE_NOSLIP;
+            if (moves && !per && !wall)
+                return fail(PLB_EINVAL, "NATIVE semantics: each axis the lattice moves along must be periodic on "
+                                        "both faces or no-slip on both faces");
+        }
+    }
+    return PLB_OK;
+}
+
+int ensure_staging(plb_solve* s) {
+    const size_t cells = (size_t)(s->p.nx + 2) * (s->p.ny + 2) * (s->p.nz + 2);
+    const size_t need = cells * (size_t)(s->q > 3 ? s->q : 3);
+    if (s->staging && s->staging_len >= need) return PLB_OK;
+    if (s->staging) { cudaFree(s->staging); s->device_bytes -= (int64_t)(s->staging_len * sizeof(float)); s->staging = nullptr; }
+    PLB_TRY(dalloc(s, (void**)&s->staging, need * sizeof(float)));
+    s->staging_len = need;
+    return PLB_OK;
+}
+
+// ---- REFERENCE semantics ---------------------------------------------------
+int ref_noslip_all(plb_solve* s) {
+    float* n = (float*)s->f[s->cur];
+    for (int i = 0; i < s->ngroups; ++i)
+        PLB_KERNEL(ref_noslip(s->q, s->g, s->fp, s->groups[i], s->group_len[i], n, s->rho, s->stream));
+    return PLB_OK;
+}
+
+int ref_boundary(plb_solve* s) {
+    PLB_TRY(ref_noslip_all(s));
+    PLB_KERNEL(ref_periodic(s->q, s->g, s->fp, (float*)s->f[s->cur], s->stream));
+    return PLB_OK;
+}
+
+int ref_one_step(plb_solve* s, bool first, bool wb_all) {
+    PLB_KERNEL(ref_fused_step(s->q, s->p.arith, first, wb_all, s->g, s->cp, s->fp, (float*)s->f[s->cur],
+                              (float*)s->f[1 - s->cur], s->rho, s->u, s->stream));
+    s->cur = 1 - s->cur;
+    return ref_boundary(s);
+}
+
+// rho/u fields = moments of n + resets, which is what plbpd holds after
+// march_in_time.
+int ref_materialize_fields(plb_solve* s) {
+    if (s->fields_valid) return PLB_OK;
+    PLB_KERNEL(ref_moments(s->q, s->g, (const float*)s->f[s->cur], s->rho, s->u, s->stream));
+    PLB_KERNEL(ref_reset(s->g, s->fp, true, true, s->rho, s->u, s->stream));
+    s->fields_valid = true;
+    return PLB_OK;
+}
+
+// ---- NATIVE semantics ------------------------------------------------------
+int nat_one_step(plb_solve* s) {
+    PLB_KERNEL(nat_fused_step(s->q, s->storage, s->p.arith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
+                              s->f[1 - s->cur], s->types, s->stream));
+    s->cur = 1 - s->cur;
+    return PLB_OK;
+}
+
+// POST -> RAW: n_t and its moments from P_{t-1}.
+int nat_materialize(plb_solve* s) {
+    if (!s->post) return PLB_OK;
+    PLB_KERNEL(nat_gather(s->q, s->storage, s->has_mask, s->g, s->np, s->f[s->cur], s->f[1 - s->cur], s->rho,
+                          s->u, s->types, s->stream));
+    s->cur = 1 - s->cur;
+    s->post = false;
+    return PLB_OK;
+}
+
+// ---- graphs of fused steps --------------------------------------------------
+int capture_chunk(plb_solve* s, int parity) {
+    cudaGraph_t graph = nullptr;
+    PLB_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = PLB_OK;
+    for (int i = 0; i < s->graph_steps && rc == PLB_OK; ++i)
+        rc = s->native ? nat_one_step(s) : ref_one_step(s, false, false);
+    const cudaError_t ec = cudaStreamEndCapture(s->stream, &graph);
+    if (rc != PLB_OK) { if (graph) cudaGraphDestroy(graph); return rc; }
+    if (ec != cudaSuccess) return fail(PLB_ECUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ec));
+    const cudaError_t ei = cudaGraphInstantiate(&s->graph[parity], graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) return fail(PLB_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ei));
+    return PLB_OK;
+}
+
+int run_chunk(plb_solve* s) {
+    const int parity = s->cur;
+    if (!s->graph[parity]) {
+        PLB_TRY(capture_chunk(s, parity));   // capture toggles cur an even number of times
+    }
+    PLB_CUDA(cudaGraphLaunch(s->graph[parity], s->stream));
+    return PLB_OK;
+}
+
+int march(plb_solve* s, int64_t n) {
+    if (n < 0) return fail(PLB_EINVAL, "negative step count");
+    if (n == 0) return PLB_OK;
+    const int64_t G = s->graph_steps;
+    if (!s->native) {
+        // the first step reads the fields when they are the caller's; the
+        // last writes every node back so the other buffer equals plbpd's ntmp
+        int64_t done = 0;
+        PLB_TRY(ref_one_step(s, s->fields_valid, n == 1));
+        done = 1;
+        while (G > 0 && n - done - 1 >= G) { PLB_TRY(run_chunk(s)); done += G; }
+        while (done < n) { PLB_TRY(ref_one_step(s, false, done == n - 1)); ++done; }
+        s->fields_valid = false;
+        return PLB_OK;
+    }
+    int64_t done = 0;
+    if (!s->post) {
+        PLB_KERNEL(nat_collide_raw(s->q, s->storage, s->p.arith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
+                                   s->f[1 - s->cur], s->rho, s->u, s->types, s->stream));
+        s->cur = 1 - s->cur;
+        s->post = true;
+        done = 1;
+    }
+    while (G > 0 && n - done >= G) { PLB_TRY(run_chunk(s)); done += G; }
+    while (done < n) { PLB_TRY(nat_one_step(s)); ++done; }
+    return PLB_OK;
+}
+
+int sync(plb_solve* s) {
+    PLB_CUDA(cudaStreamSynchronize(s->stream));
+    return PLB_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+const char* plb_last_error(void) { return g_last_error.c_str(); }
+
+int plb_version(void) { return 10000; }
+
+int plb_model_tables(const char* name, int32_t* c, float* w, uint32_t* rev, float* cs2) {
+    if (!name) return fail(PLB_EINVAL, "model name is null");
+    const std::string n(name);
+    const int q = n == "D2Q9" ? 9 : n == "D3Q19" ? 19 : n == "D3Q27" ? 27 : 0;
+    if (!q) return fail(PLB_EINVAL, "Model " + n + " not yet implemented");
+    tables(q, c, w, rev);
+    if (cs2) *cs2 = (float)(1. / 3.);
+    return q;
+}
+
+int plb_equilibrium(int32_t q, float rho, const float* u3, float* out_q) {
+    if (!tables(q, nullptr, nullptr, nullptr)) return fail(PLB_EINVAL, "invalid Q");
+    if (!u3 || !out_q) return fail(PLB_EINVAL, "null pointer");
+    host_eqlb(q, rho, u3, out_q);
+    return PLB_OK;
+}
+
+int plb_relaxation(float nu, float* tau, float* omega) {
+    float t, o;
+    relaxation(nu, &t, &o);
+    if (tau) *tau = t;
+    if (omega) *omega = o;
+    return PLB_OK;
+}
+
+int plb_solve_create(const plb_params* params, plb_solve** out) {
+    if (!out) return fail(PLB_EINVAL, "out is null");
+    *out = nullptr;
+    PLB_TRY(validate(params));
+    plb_solve* s = new plb_solve();
+    s->p = *params;
+    s->q = params->q;
+    s->native = params->semantics == PLB_SEMANTICS_NATIVE;
+    s->storage = params->storage;
+    s->graph_steps = graph_steps_default();
+    int rc = PLB_OK;
+    auto bail = [&](int code) { release(s); return code; };
+    {
+        const cudaError_t e = cudaSetDevice(params->device);
+        if (e != cudaSuccess) return bail(fail(PLB_ECUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e)));
+    }
+    // geometry
+    Geo& g = s->g;
+    g.nx = (int)params->nx; g.ny = (int)params->ny; g.nz = (int)params->nz;
+    const size_t esize = s->storage == PLB_STORAGE_FP16_DEV ? 2 : 4;
+    if (s->native) {
+        g.h = 0; g.xoff = 0;
+        g.ys = round_up(g.nx, 32 / (long long)esize);
+        g.zs = g.ys * g.ny;
+        g.fs = g.zs * g.nz;
+        g.ks = round_up(g.fs, 128);
+        g.wrap_x = params->face_type[0] == PLB_FACE_PERIODIC && params->face_type[1] == PLB_FACE_PERIODIC;
+        g.wrap_y = params->face_type[2] == PLB_FACE_PERIODIC && params->face_type[3] == PLB_FACE_PERIODIC;
+        g.wrap_z = params->face_type[4] == PLB_FACE_PERIODIC && params->face_type[5] == PLB_FACE_PERIODIC;
+    } else {
+        g.h = 1; g.xoff = 8;
+        g.ys = round_up(g.xoff + g.nx + 1, 8);
+        g.zs = g.ys * (g.ny + 2);
+        g.fs = g.zs * (g.nz + 2);
+        g.ks = round_up(g.fs, 64);
+    }
+    // collision and boundary parameters, derived as plbpd derives them
+    relaxation(params->nu, &s->cp.tau, &s->cp.omega);
+    s->cp.omc = 1.0f - s->cp.omega;
+    s->cp.fx = params->force[0]; s->cp.fy = params->force[1]; s->cp.fz = params->force[2];
+    const float cs2 = (float)(1. / 3.);
+    const float cs2inv = 1.0f / cs2;   // src/Boundary.cpp:27
+    s->fp.noslip_mask = 0; s->fp.vel_mask = 0;
+    for (int f = 0; f < 6; ++f) {
+        if (params->face_type[f] == PLB_FACE_NOSLIP) s->fp.noslip_mask |= 1 << f;
+        if (params->face_has_vel[f]) s->fp.vel_mask |= 1 << f;
+        for (int i = 0; i < 3; ++i) s->fp.vel[f][i] = params->face_has_vel[f] ? params->face_vel[f][i] : 0.0f;
+    }
+    s->fp.rho_solid = params->rho_solid;
+    s->fp.cs2inv = cs2inv;
+    s->fp.ew_periodic = params->face_type[0] == PLB_FACE_PERIODIC && params->face_type[1] == PLB_FACE_PERIODIC;
+    s->fp.ns_periodic = params->face_type[2] == PLB_FACE_PERIODIC && params->face_type[3] == PLB_FACE_PERIODIC;
+    std::memset(&s->np, 0, sizeof(s->np));
+    for (int f = 0; f < 6; ++f)
+        for (int i = 0; i < 3; ++i) s->np.vel[f][i] = s->fp.vel[f][i];
+    s->np.rho_solid = params->rho_solid;
+    s->np.cs2inv = cs2inv;
+    // no-slip launch groups: faces in plbpd's order; two parallel faces share
+    // a launch when they are far enough apart not to touch the same slots
+    {
+        const long long ext[3] = {params->nx, params->ny, params->nz};
+        int f = 0;
+        while (f < 6) {
+            if (!((s->fp.noslip_mask >> f) & 1)) { ++f; continue; }
+            const int axis = f / 2;
+            if ((f % 2) == 0 && ((s->fp.noslip_mask >> (f + 1)) & 1) && ext[axis] >= 4) {
+                s->groups[s->ngroups][0] = f; s->groups[s->ngroups][1] = f + 1; s->group_len[s->ngroups++] = 2;
+                f += 2;
+            } else {
+                s->groups[s->ngroups][0] = f; s->group_len[s->ngroups++] = 1;
+                f += 1;
+            }
+        }
+    }
+    // device memory
+    {
+        const cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return bail(fail(PLB_ECUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)));
+    }
+    const size_t pop_bytes = (size_t)s->q * (size_t)g.ks * esize;
+    if ((rc = dalloc(s, &s->f[0], pop_bytes)) != PLB_OK) return bail(rc);
+    if ((rc = dalloc(s, &s->f[1], pop_bytes)) != PLB_OK) return bail(rc);
+    if ((rc = dalloc(s, (void**)&s->rho, (size_t)g.ks * sizeof(float))) != PLB_OK) return bail(rc);
+    if ((rc = dalloc(s, (void**)&s->u, 3 * (size_t)g.ks * sizeof(float))) != PLB_OK) return bail(rc);
+    if ((rc = dalloc(s, (void**)&s->consts, 2 * 27 * sizeof(float))) != PLB_OK) return bail(rc);
+    if ((rc = dalloc(s, (void**)&s->partials, (size_t)util_conservation_partials() * sizeof(double))) != PLB_OK)
+        return bail(rc);
+    if ((rc = dalloc(s, (void**)&s->out4, 4 * sizeof(double))) != PLB_OK) return bail(rc);
+    if (cudaHostAlloc((void**)&s->out4_host, 4 * sizeof(double), cudaHostAllocDefault) != cudaSuccess)
+        return bail(fail(PLB_ENOMEM, "cudaHostAlloc failed"));
+    {
+        // plbpd's SimData starts every field at 0 (src/SimData.cpp:53-56)
+        cudaError_t e = cudaSuccess;
+        if (e == cudaSuccess) e = cudaMemsetAsync(s->f[0], 0, pop_bytes, s->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s->f[1], 0, pop_bytes, s->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s->rho, 0, (size_t)g.ks * sizeof(float), s->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s->u, 0, 3 * (size_t)g.ks * sizeof(float), s->stream);
+        if (e != cudaSuccess) return bail(fail(PLB_ECUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e)));
+    }
+    {
+        // consts: EqlbDist(rho0, u0), then the weights
+        float host[54];
+        host_eqlb(s->q, params->rho0, params->u0, host);
+        tables(s->q, nullptr, host + s->q, nullptr);
+        if (cudaMemcpyAsync(s->consts, host, 2 * s->q * sizeof(float), cudaMemcpyHostToDevice, s->stream) !=
+            cudaSuccess)
+            return bail(fail(PLB_ECUDA, "cudaMemcpyAsync(consts)"));
+    }
+    if (s->native) {
+        s->has_mask = s->fp.noslip_mask != 0;
+        if ((rc = dalloc(s, (void**)&s->types, (size_t)g.ks)) != PLB_OK) return bail(rc);
+        if ((rc = dalloc(s, (void**)&s->types_tmp, (size_t)g.ks)) != PLB_OK) return bail(rc);
+        if (cudaMemsetAsync(s->types, 0, (size_t)g.ks, s->stream) != cudaSuccess)
+            return bail(fail(PLB_ECUDA, "cudaMemsetAsync(types)"));
+        const int e = nat_build_types(s->q, g, nullptr, s->fp.noslip_mask, s->types_tmp, s->types, s->stream);
+        if (e != 0) return bail(fail(PLB_ECUDA, "nat_build_types"));
+        s->post = false;
+    }
+    s->fields_valid = true;
+    if (cudaStreamSynchronize(s->stream) != cudaSuccess) return bail(fail(PLB_ECUDA, "solve setup failed"));
+    *out = s;
+    return PLB_OK;
+}
+
+int plb_solve_destroy(plb_solve* s) {
+    if (!s) return PLB_OK;
+    set_device(s);
+    cudaStreamSynchronize(s->stream);
+    release(s);
+    return PLB_OK;
+}
+
+int plb_set_mask(plb_solve* s, const uint8_t* mask) {
+    if (!s) return fail(PLB_EINVAL, "solve is null");
+    if (!s->native) return fail(PLB_EUNSUPPORTED, "obstacle masks need NATIVE semantics");
+    PLB_TRY(set_device(s));
+    PLB_TRY(nat_materialize(s));
+    const size_t cells = (size_t)s->g.cells();
+    if (!s->mask_dev) PLB_TRY(dalloc(s, (void**)&s->mask_dev, cells));
+    if (mask) PLB_CUDA(cudaMemcpyAsync(s->mask_dev, mask, cells, cudaMemcpyHostToDevice, s->stream));
+    PLB_KERNEL(nat_build_types(s->q, s->g, mask ? s->mask_dev : nullptr, s->fp.noslip_mask, s->types_tmp, s->types,
+                               s->stream));
+    s->has_mask = mask != nullptr || s->fp.noslip_mask != 0;
+    drop_graphs(s);
+    return sync(s);
+}
+
+int plb_initialize(plb_solve* s) {
+    if (!s) return fail(PLB_EINVAL, "solve is null");
+    PLB_TRY(set_device(s));
+    s->cur = 0;
+    PLB_KERNEL(util_init_uniform(s->q, s->storage, s->g, s->consts, s->p.rho0, s->p.u0, s->f[0], s->f[1], s->rho,
+                                 s->u, s->stream));
+    if (s->native) {
+        if (s->has_mask) PLB_KERNEL(nat_reset_fields(s->g, s->np, s->types, s->rho, s->u, s->stream));
+        s->post = false;
+    } else {
+        PLB_KERNEL(ref_reset(s->g, s->fp, true, true, s->rho, s->u, s->stream));
+        s->fields_valid = true;
+    }
+    return sync(s);
+}
+
+int plb_step_async(plb_solve* s, int64_t nsteps) {
+    if (!s) return fail(PLB_EINVAL, "solve is null");
+    PLB_TRY(set_device(s));
+    return march(s, nsteps);
+}
+
+int plb_step(plb_solve* s, int64_t nsteps) {
+    PLB_TRY(plb_step_async(s, nsteps));
+    return sync(s);
+}
+
+int plb_synchronize(plb_solve* s) {
+    if (!s) return fail(PLB_EINVAL, "solve is null");
+    PLB_TRY(set_device(s));
+    return sync(s);
+}
+
+void* plb_stream_handle(plb_solve* s) { return s ? (void*)s->stream : nullptr; }
+
+// ---- unfused operators ------------------------------------------------------
+#define PLB_REF_ONLY(s)                                                                   \
+    do {                                                                                  \
+        if (!(s)) return fail(PLB_EINVAL, "solve is null");                               \
+        if ((s)->native) return fail(PLB_EUNSUPPORTED, "operator needs REFERENCE semantics"); \
+        PLB_TRY(set_device(s));                                                           \
+        PLB_TRY(ref_materialize_fields(s));                                               \
+    } while (0)
+
+int plb_collide(plb_solve* s) {
+    PLB_REF_ONLY(s);
+    PLB_KERNEL(ref_collide(s->q, s->p.arith, s->g, s->cp, (float*)s->f[s->cur], s->rho, s->u, s->stream));
+    return sync(s);
+}
+
+int plb_stream_push(plb_solve* s) {
+    PLB_REF_ONLY(s);
+    PLB_KERNEL(ref_push(s->q, s->g, (const float*)s->f[s->cur], (float*)s->f[1 - s->cur], s->stream));
+    s->cur = 1 - s->cur;
+    return sync(s);
+}
+
+int plb_apply_noslip(plb_solve* s) {
+    PLB_REF_ONLY(s);
+    PLB_TRY(ref_noslip_all(s));
+    return sync(s);
+}
+
+int plb_apply_periodicity(plb_solve* s) {
+    PLB_REF_ONLY(s);
+    PLB_KERNEL(ref_periodic(s->q, s->g, s->fp, (float*)s->f[s->cur], s->stream));
+    return sync(s);
+}
+
+int plb_calc_moments(plb_solve* s) {
+    PLB_REF_ONLY(s);
+    PLB_KERNEL(ref_moments(s->q, s->g, (const float*)s->f[s->cur], s->rho, s->u, s->stream));
+    return sync(s);
+}
+
+int plb_reset(plb_solve* s) {
+    PLB_REF_ONLY(s);
+    PLB_KERNEL(ref_reset(s->g, s->fp, true, true, s->rho, s->u, s->stream));
+    return sync(s);
+}
+
+int plb_reset_velocity(plb_solve* s) {
+    PLB_REF_ONLY(s);
+    PLB_KERNEL(ref_reset(s->g, s->fp, true, false, s->rho, s->u, s->stream));
+    return sync(s);
+}
+
+int plb_reset_density(plb_solve* s) {
+    PLB_REF_ONLY(s);
+    PLB_KERNEL(ref_reset(s->g, s->fp, false, true, s->rho, s->u, s->stream));
+    return sync(s);
+}
+
+// ---- transfers ----------------------------------------------------------------
+size_t plb_field_len(const plb_solve* s, int32_t which) {
+    if (!s) return 0;
+    const size_t cells = (size_t)(s->p.nx + 2) * (s->p.ny + 2) * (s->p.nz + 2);
+    switch (which) {
+        case PLB_FIELD_N: case PLB_FIELD_NTMP: return cells * (size_t)s->q;
+        case PLB_FIELD_RHO: return cells;
+        case PLB_FIELD_U: return cells * 3;
+        default: return 0;
+    }
+}
+
+int plb_get_field(plb_solve* s, int32_t which, float* out) {
+    if (!s || !out) return fail(PLB_EINVAL, "null argument");
+    if (which < PLB_FIELD_N || which > PLB_FIELD_U) return fail(PLB_EINVAL, "invalid field id");
+    PLB_TRY(set_device(s));
+    const size_t len = plb_field_len(s, which);
+    if (s->native) {
+        if (which == PLB_FIELD_NTMP) { std::memset(out, 0, len * sizeof(float)); return PLB_OK; }
+        PLB_TRY(nat_materialize(s));
+    } else if (which == PLB_FIELD_RHO || which == PLB_FIELD_U) {
+        PLB_TRY(ref_materialize_fields(s));
+    }
+    PLB_TRY(ensure_staging(s));
+    const float* wk = s->consts + s->q;
+    if (which == PLB_FIELD_N || which == PLB_FIELD_NTMP) {
+        const void* src = s->f[which == PLB_FIELD_N ? s->cur : 1 - s->cur];
+        PLB_KERNEL(util_export(s->storage, s->q, s->g, src, wk, s->staging, s->stream));
+    } else {
+        PLB_KERNEL(util_export(0, which == PLB_FIELD_RHO ? 1 : 3, s->g, which == PLB_FIELD_RHO ? s->rho : s->u,
+                               nullptr, s->staging, s->stream));
+    }
+    PLB_CUDA(cudaMemcpyAsync(out, s->staging, len * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    return sync(s);
+}
+
+int plb_set_field(plb_solve* s, int32_t which, const float* in) {
+    if (!s || !in) return fail(PLB_EINVAL, "null argument");
+    if (which < PLB_FIELD_N || which > PLB_FIELD_U) return fail(PLB_EINVAL, "invalid field id");
+    PLB_TRY(set_device(s));
+    if (s->native) {
+        if (which == PLB_FIELD_NTMP) return PLB_OK;   // NATIVE keeps no second population state
+        PLB_TRY(nat_materialize(s));
+    } else {
+        PLB_TRY(ref_materialize_fields(s));
+    }
+    PLB_TRY(ensure_staging(s));
+    const size_t len = plb_field_len(s, which);
+    PLB_CUDA(cudaMemcpyAsync(s->staging, in, len * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    if (which == PLB_FIELD_N || which == PLB_FIELD_NTMP) {
+        void* dst = s->f[which == PLB_FIELD_N ? s->cur : 1 - s->cur];
+        PLB_KERNEL(util_import(s->storage, s->q, s->g, s->staging, s->consts + s->q, dst, s->stream));
+    } else {
+        PLB_KERNEL(util_import(0, which == PLB_FIELD_RHO ? 1 : 3, s->g, s->staging, nullptr,
+                               which == PLB_FIELD_RHO ? (void*)s->rho : (void*)s->u, s->stream));
+        if (!s->native) s->fields_valid = true;
+    }
+    return sync(s);
+}
+
+int plb_conservation(plb_solve* s, double* out4) {
+    if (!s || !out4) return fail(PLB_EINVAL, "null argument");
+    PLB_TRY(set_device(s));
+    PLB_KERNEL(util_conservation(s->q, s->storage, s->g, s->f[s->cur], s->native ? s->types : nullptr,
+                                 s->fp.noslip_mask, s->partials, s->out4, s->stream));
+    PLB_CUDA(cudaMemcpyAsync(s->out4_host, s->out4, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    PLB_TRY(sync(s));
+    std::memcpy(out4, s->out4_host, 4 * sizeof(double));
+    return PLB_OK;
+}
+
+int plb_host_alloc(size_t bytes, void** out) {
+    if (!out) return fail(PLB_EINVAL, "out is null");
+    PLB_CUDA(cudaHostAlloc(out, bytes, cudaHostAllocDefault));
+    return PLB_OK;
+}
+
+int plb_host_free(void* p) {
+    if (p) PLB_CUDA(cudaFreeHost(p));
+    return PLB_OK;
+}
+
+int64_t plb_device_bytes(const plb_solve* s) { return s ? s->device_bytes : 0; }
+
+}  // extern "C"

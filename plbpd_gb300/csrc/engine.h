@@ -1,0 +1,99 @@
+// Internal interface between the C ABI (capi.cu) and the kernel files.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "lattice.cuh"
+
+namespace plb {
+
+// Boundary description handed to the REFERENCE-semantics kernels.  Faces are
+// numbered east, west, north, south, up, down (plbpd's src/Boundary.cpp:17-18).
+struct FaceParams {
+    int noslip_mask;      // bit f: face f is a no-slip wall
+    int vel_mask;         // bit f: face f has a velocity entry
+    float vel[6][3];      // u_b per face
+    float rho_solid;
+    float cs2inv;         // 1.0f / c_s^2 (src/Boundary.cpp:27)
+    int ew_periodic, ns_periodic;
+};
+
+// Node types under NATIVE semantics (one byte per interior node).
+//   bit 7: solid; bits 0-2 then index the solid's wall velocity (0..5 = face,
+//          6 = obstacle, zero velocity)
+//   bit 6: fluid node with at least one solid neighbour
+enum : uint8_t { kSolid = 0x80, kNearSolid = 0x40, kVelMask = 0x07, kObstacleVel = 6 };
+
+struct NativeParams {
+    float vel[8][3];      // solid velocities by index (6 = obstacle = 0)
+    float rho_solid;
+    float cs2inv;
+};
+
+// ---- REFERENCE semantics (kernels_ref.cu) ----------------------------------
+// One fused step: moments (or the rho/u fields when `first`), resets, collision
+// and push into `nxt`; boundary-layer nodes also write their collided values
+// back into `cur` (every node when `wb_all`).  Returns a cudaError_t.
+int ref_fused_step(int q, int arith, bool first, bool wb_all, const Geo& g, const CollideParams& cp,
+                   const FaceParams& fp, float* cur, float* nxt, float* rho, float* u,
+                   cudaStream_t st);
+// No-slip for the faces in face_list[0..nfaces) in one launch (faces must not
+// interact; the host groups them).
+int ref_noslip(int q, const Geo& g, const FaceParams& fp, const int* face_list, int nfaces,
+               float* n, const float* rho, cudaStream_t st);
+// East/west then north/south halo copies, as one launch.
+int ref_periodic(int q, const Geo& g, const FaceParams& fp, float* n, cudaStream_t st);
+// Unfused operators.
+int ref_collide(int q, int arith, const Geo& g, const CollideParams& cp, float* n,
+                const float* rho, const float* u, cudaStream_t st);
+int ref_push(int q, const Geo& g, const float* n, float* nt, cudaStream_t st);
+int ref_moments(int q, const Geo& g, const float* n, float* rho, float* u, cudaStream_t st);
+int ref_reset(const Geo& g, const FaceParams& fp, bool velocity, bool density, float* rho,
+              float* u, cudaStream_t st);
+
+// ---- NATIVE semantics (kernels_native.cu) ---------------------------------
+// storage: 0 = FP32, 1 = FP16 deviations f - w.
+// Collision of a RAW state (n in `src`, rho/u fields), result P into `dst`.
+int nat_collide_raw(int q, int storage, int arith, bool has_mask, const Geo& g,
+                    const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
+                    const float* rho, const float* u, const uint8_t* types, cudaStream_t st);
+// One fused step: gather P from `src` (streaming + bounce-back), moments,
+// collision, store P into `dst`.
+int nat_fused_step(int q, int storage, int arith, bool has_mask, const Geo& g,
+                   const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
+                   const uint8_t* types, cudaStream_t st);
+// Gather only: writes n (storage format, or nullptr) and the moments with the
+// solid-node resets (rho/u, or nullptr).
+int nat_gather(int q, int storage, bool has_mask, const Geo& g, const NativeParams& np,
+               const void* src, void* n_out, float* rho, float* u, const uint8_t* types,
+               cudaStream_t st);
+// Solid nodes' fields = (rho_solid, wall velocity).
+int nat_reset_fields(const Geo& g, const NativeParams& np, const uint8_t* types, float* rho,
+                     float* u, cudaStream_t st);
+// Node types from an obstacle mask (nz*ny*nx bytes, may be null) and the walls.
+// `scratch` has the size of `types`.
+int nat_build_types(int q, const Geo& g, const uint8_t* mask, int noslip_mask,
+                    uint8_t* scratch, uint8_t* types, cudaStream_t st);
+
+// ---- shared (kernels_util.cu) ----------------------------------------------
+// Every node of the box (halo included): rho0, u0, n = feq, ntmp = 0.
+// `feq_dev` is a device array of 2q floats: the equilibrium, then the weights.
+// u0 is a host array.  `nt` may be null.
+int util_init_uniform(int q, int storage, const Geo& g, const float* feq_dev, float rho0,
+                      const float* u0, void* n, void* nt, float* rho, float* u,
+                      cudaStream_t st);
+// Device layout <-> plbpd's AoS halo layout (`aos` is a device buffer of
+// (nx+2)(ny+2)(nz+2)*v floats).  Halo slots the device does not hold read as
+// 0.  Under FP16 storage (populations only) `wk` are the v weights (device).
+int util_export(int storage, int v, const Geo& g, const void* src, const float* wk, float* aos,
+                cudaStream_t st);
+int util_import(int storage, int v, const Geo& g, const float* aos, const float* wk, void* dst,
+                cudaStream_t st);
+// FP64 sums of n_k and n_k c_k over fluid nodes.  `partials` holds at least
+// util_conservation_partials() doubles; out4 is a device pointer.
+int util_conservation_partials();
+int util_conservation(int q, int storage, const Geo& g, const void* n, const uint8_t* types,
+                      int noslip_mask, double* partials, double* out4, cudaStream_t st);
+
+}  // namespace plb

@@ -1,0 +1,396 @@
+// Kernels for NATIVE semantics: one fused pull kernel per time step.
+//
+// The device holds P, the post-collision populations of the previous step.
+// A step at node x gathers n[x][k] = P[x - c_k][k] (periodic axes wrap), or,
+// when x - c_k is solid, the bounce-back value P[x][rev k] that node x itself
+// stored with the moving-wall term already applied; then it computes the
+// moments, collides and stores P[x][k] at its own node.  Reads of a shifted
+// row are misaligned by one element, writes are whole aligned sectors.
+//
+// The bounce-back is plbpd's no-slip rule (src/Boundary.cpp:189-221) for a
+// fluid node next to a solid one:
+//   n[x][rev k] = P[x][k] - 2 w_k rho[x] (c_k . u_b) / c_s^2,  x + c_k solid,
+// with rho[x] the density node x collided with -- available in registers when
+// P[x][k] is stored, so the term is applied on the store side.
+//
+// Storage: FP32 populations, or FP16 deviations d_k = f_k - w_k with all
+// arithmetic in FP32 (the deviation form keeps the small part of f_k).
+#include "engine.h"
+
+namespace plb {
+namespace {
+
+constexpr int kBlockX = 128;
+
+template <int ST> struct Store;
+template <> struct Store<0> {
+    using T = float;
+    __device__ static __forceinline__ float ld(const float* p, long long i) { return __ldg(p + i); }
+    __device__ static __forceinline__ void st(float* p, long long i, float v) { __stcs(p + i, v); }
+};
+template <> struct Store<1> {
+    using T = __half;
+    __device__ static __forceinline__ float ld(const __half* p, long long i) { return __half2float(__ldg(p + i)); }
+    __device__ static __forceinline__ void st(__half* p, long long i, float v) { __stcs(reinterpret_cast<unsigned short*>(p) + i, __half_as_ushort(__float2half_rn(v))); }
+};
+
+// Neighbour index helper: element offsets of x-1, x, x+1 (and y, z) with the
+// periodic axes wrapped.  A fluid node never has a neighbour outside the box
+// along a walled axis, because the wall layer in between is solid.
+struct Nbr {
+    long long xo[3], yo[3], zo[3];
+    __device__ __forceinline__ Nbr(const Geo& g, int x, int y, int z) {
+        const int xm = (x == 0 && g.wrap_x) ? g.nx - 1 : x - 1;
+        const int xp = (x == g.nx - 1 && g.wrap_x) ? 0 : x + 1;
+        const int ym = (y == 0 && g.wrap_y) ? g.ny - 1 : y - 1;
+        const int yp = (y == g.ny - 1 && g.wrap_y) ? 0 : y + 1;
+        const int zm = (z == 0 && g.wrap_z) ? g.nz - 1 : z - 1;
+        const int zp = (z == g.nz - 1 && g.wrap_z) ? 0 : z + 1;
+        xo[0] = xm + g.xoff; xo[1] = x + g.xoff; xo[2] = xp + g.xoff;
+        yo[0] = (long long)ym * g.ys; yo[1] = (long long)y * g.ys; yo[2] = (long long)yp * g.ys;
+        zo[0] = (long long)zm * g.zs; zo[1] = (long long)z * g.zs; zo[2] = (long long)zp * g.zs;
+    }
+    // node at x + s*c_k, s = +1 (downstream) or -1 (upstream)
+    template <int Q>
+    __device__ __forceinline__ long long at(int k, int s) const {
+        return zo[1 + s * Lattice<Q>::cz(k)] + yo[1 + s * Lattice<Q>::cy(k)] + xo[1 + s * Lattice<Q>::cx(k)];
+    }
+};
+
+// Collision in deviation form for FP16 storage.  d_k = f_k - w_k,
+// drho = sum d_k, rho = 1 + drho, and
+//   f_eq,k - w_k = w_k (drho + rho (3 cu + 4.5 cu^2 - 1.5 usq)),
+//   d'_k = (1 - omega) d_k + omega (f_eq,k - w_k).
+template <int Q>
+__device__ __forceinline__ void collide_node_dev(float (&d)[Q], float drho, float rho, float ux, float uy,
+                                                 float uz, const CollideParams& P) {
+    const float tr = __fdiv_rn(P.tau, rho);
+    const float vx = __fadd_rn(ux, __fmul_rn(P.fx, tr));
+    const float vy = __fadd_rn(uy, __fmul_rn(P.fy, tr));
+    const float vz = __fadd_rn(uz, __fmul_rn(P.fz, tr));
+    const float usq = __fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz));
+    const float kusq = __fmul_rn(-1.5f, usq);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        const float cu = (k == 0) ? 0.0f : dot_c<Q>(k, vx, vy, vz);
+        float t = __fmaf_rn(4.5f, __fmul_rn(cu, cu), kusq);
+        t = __fmaf_rn(3.0f, cu, t);
+        float e = __fmaf_rn(rho, t, drho);
+        e = __fmul_rn(weight<Q>(k), e);
+        d[k] = __fmaf_rn(P.omc, d[k], __fmul_rn(P.omega, e));
+    }
+}
+
+// Moments in deviation form: drho = sum d_k, j = sum c_k d_k,
+// u = j / (1 + drho).
+template <int Q>
+__device__ __forceinline__ void node_moments_dev(const float (&d)[Q], float& drho, float& rho, float& ux,
+                                                 float& uy, float& uz) {
+    float jx, jy, jz;
+    node_sums<Q>(d, drho, jx, jy, jz);
+    rho = __fadd_rn(1.0f, drho);
+    const float rinv = __fdiv_rn(1.0f, rho);
+    ux = __fmul_rn(jx, rinv);
+    uy = __fmul_rn(jy, rinv);
+    uz = __fmul_rn(jz, rinv);
+}
+
+// Stores the collided populations of a fluid node; a direction that points
+// into a solid node becomes the bounce-back slot and carries the moving-wall
+// term (src/Boundary.cpp:215-217).
+template <int Q, int ST, bool MASK>
+__device__ __forceinline__ void store_node(typename Store<ST>::T* __restrict__ dst, const Geo& g,
+                                           const NativeParams& np, const uint8_t* __restrict__ types,
+                                           const Nbr& nb, long long node, bool near, float rho,
+                                           const float (&f)[Q]) {
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        float v = f[k];
+        if (MASK && near && k != 0) {
+            const uint8_t t = __ldg(types + nb.at<Q>(k, +1));
+            if (t & kSolid)
+                v = __fsub_rn(v, wall_term<Q>(k, rho, dot_c_full<Q>(k, np.vel[t & kVelMask]), np.cs2inv));
+        }
+        Store<ST>::st(dst, k * g.ks + node, v);
+    }
+}
+
+// Gathers n[x][*] from P (streaming plus bounce-back).
+template <int Q, int ST, bool MASK>
+__device__ __forceinline__ void gather_node(const typename Store<ST>::T* __restrict__ src, const Geo& g,
+                                            const uint8_t* __restrict__ types, const Nbr& nb,
+                                            long long node, bool near, float (&f)[Q]) {
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        long long s = nb.at<Q>(k, -1);
+        int kk = k;
+        if (MASK && near && k != 0) {
+            if (__ldg(types + s) & kSolid) { s = node; kk = rev_of(k); }
+        }
+        f[k] = Store<ST>::ld(src, kk * g.ks + s);
+    }
+}
+
+// ---------------------------------------------------------------------------
+template <int Q, int ST, bool MASK, int ARITH>
+__global__ void __launch_bounds__(kBlockX)
+nat_fused_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::T* __restrict__ src,
+            typename Store<ST>::T* __restrict__ dst, const uint8_t* __restrict__ types) {
+    const int x = blockIdx.x * kBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
+    const long long node = g.idx(x, y, z);
+    bool near = false;
+    if (MASK) {
+        const uint8_t t = __ldg(types + node);
+        if (t & kSolid) return;
+        near = (t & kNearSolid) != 0;
+    }
+    const Nbr nb(g, x, y, z);
+    float f[Q];
+    gather_node<Q, ST, MASK>(src, g, types, nb, node, near, f);
+    float rho;
+    if (ST == 0) {
+        float ux, uy, uz;
+        node_moments<Q>(f, rho, ux, uy, uz);
+        collide_node<Q, ARITH>(f, rho, ux, uy, uz, cp);
+    } else {
+        float drho, ux, uy, uz;
+        node_moments_dev<Q>(f, drho, rho, ux, uy, uz);
+        collide_node_dev<Q>(f, drho, rho, ux, uy, uz, cp);
+    }
+    store_node<Q, ST, MASK>(dst, g, np, types, nb, node, near, rho, f);
+}
+
+// First collision from a RAW state: n at the node itself and the rho/u fields.
+template <int Q, int ST, bool MASK, int ARITH>
+__global__ void __launch_bounds__(kBlockX)
+nat_collide_raw_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::T* __restrict__ src,
+                  typename Store<ST>::T* __restrict__ dst, const float* __restrict__ rho_f,
+                  const float* __restrict__ u_f, const uint8_t* __restrict__ types) {
+    const int x = blockIdx.x * kBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
+    const long long node = g.idx(x, y, z);
+    bool near = false;
+    if (MASK) {
+        const uint8_t t = __ldg(types + node);
+        if (t & kSolid) return;
+        near = (t & kNearSolid) != 0;
+    }
+    const Nbr nb(g, x, y, z);
+    float f[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) f[k] = Store<ST>::ld(src, k * g.ks + node);
+    const float rho = rho_f[node];
+    const float ux = u_f[node], uy = u_f[g.ks + node], uz = u_f[2 * g.ks + node];
+    if (ST == 0) collide_node<Q, ARITH>(f, rho, ux, uy, uz, cp);
+    else collide_node_dev<Q>(f, __fsub_rn(rho, 1.0f), rho, ux, uy, uz, cp);
+    store_node<Q, ST, MASK>(dst, g, np, types, nb, node, near, rho, f);
+}
+
+// Gather only: n (storage format) and/or moments, solid nodes reset to
+// (rho_solid, u_b) as Boundary::reset does for walls.
+template <int Q, int ST, bool MASK>
+__global__ void __launch_bounds__(kBlockX)
+nat_gather_k(Geo g, NativeParams np, const typename Store<ST>::T* __restrict__ src,
+             typename Store<ST>::T* __restrict__ n_out, float* __restrict__ rho_f,
+             float* __restrict__ u_f, const uint8_t* __restrict__ types) {
+    const int x = blockIdx.x * kBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
+    const long long node = g.idx(x, y, z);
+    bool near = false;
+    if (MASK) {
+        const uint8_t t = __ldg(types + node);
+        if (t & kSolid) {
+            if (rho_f) {
+                const float* ub = np.vel[t & kVelMask];
+                rho_f[node] = np.rho_solid;
+                u_f[node] = ub[0]; u_f[g.ks + node] = ub[1]; u_f[2 * g.ks + node] = ub[2];
+            }
+            if (n_out) {
+#pragma unroll
+                for (int k = 0; k < Q; ++k) Store<ST>::st(n_out, k * g.ks + node, ST == 0 ? 0.0f : -weight<Q>(k));
+            }
+            return;
+        }
+        near = (t & kNearSolid) != 0;
+    }
+    const Nbr nb(g, x, y, z);
+    float f[Q];
+    gather_node<Q, ST, MASK>(src, g, types, nb, node, near, f);
+    if (n_out) {
+#pragma unroll
+        for (int k = 0; k < Q; ++k) Store<ST>::st(n_out, k * g.ks + node, f[k]);
+    }
+    if (rho_f) {
+        float rho, ux, uy, uz;
+        if (ST == 0) node_moments<Q>(f, rho, ux, uy, uz);
+        else { float drho; node_moments_dev<Q>(f, drho, rho, ux, uy, uz); }
+        rho_f[node] = rho;
+        u_f[node] = ux; u_f[g.ks + node] = uy; u_f[2 * g.ks + node] = uz;
+    }
+}
+
+// Node types: solid from the mask or a wall layer (velocity index = the last
+// wall face in plbpd's face order, else obstacle); fluid nodes with a solid
+// neighbour along any lattice direction are marked near-solid.
+template <int Q>
+__global__ void __launch_bounds__(kBlockX)
+nat_types_solid_k(Geo g, const uint8_t* __restrict__ mask, int noslip_mask, uint8_t* __restrict__ types) {
+    const int x = blockIdx.x * kBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
+    uint8_t t = 0;
+    if (mask && mask[((long long)z * g.ny + y) * g.nx + x]) t = kSolid | kObstacleVel;
+    const bool in[6] = {x == g.nx - 1, x == 0, y == g.ny - 1, y == 0, z == g.nz - 1, z == 0};
+    for (int f = 0; f < 6; ++f)
+        if (((noslip_mask >> f) & 1) && in[f]) t = kSolid | (uint8_t)f;
+    types[g.idx(x, y, z)] = t;
+}
+
+template <int Q>
+__global__ void __launch_bounds__(kBlockX)
+nat_types_near_k(Geo g, const uint8_t* __restrict__ types, uint8_t* __restrict__ out) {
+    const int x = blockIdx.x * kBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
+    const long long node = g.idx(x, y, z);
+    const uint8_t t = types[node];
+    out[node] = t;
+    if (t & kSolid) return;
+    const Nbr nb(g, x, y, z);
+    bool near = false;
+#pragma unroll
+    for (int k = 1; k < Q; ++k) {
+        const int xx = x + Lattice<Q>::cx(k), yy = y + Lattice<Q>::cy(k), zz = z + Lattice<Q>::cz(k);
+        const bool inside = (g.wrap_x || (xx >= 0 && xx < g.nx)) && (g.wrap_y || (yy >= 0 && yy < g.ny)) &&
+                            (g.wrap_z || (zz >= 0 && zz < g.nz));
+        if (inside && (types[nb.at<Q>(k, +1)] & kSolid)) near = true;
+    }
+    if (near) out[node] = t | kNearSolid;
+}
+
+// Solid nodes' fields: rho_solid and the wall velocity, as Boundary::reset
+// leaves wall nodes (src/Boundary.cpp:58-89).
+__global__ void __launch_bounds__(kBlockX)
+nat_reset_fields_k(Geo g, NativeParams np, const uint8_t* __restrict__ types, float* __restrict__ rho_f,
+                   float* __restrict__ u_f) {
+    const int x = blockIdx.x * kBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
+    const long long node = g.idx(x, y, z);
+    const uint8_t t = types[node];
+    if (!(t & kSolid)) return;
+    const float* ub = np.vel[t & kVelMask];
+    rho_f[node] = np.rho_solid;
+    u_f[node] = ub[0]; u_f[g.ks + node] = ub[1]; u_f[2 * g.ks + node] = ub[2];
+}
+
+dim3 cell_grid(const Geo& g) { return dim3((g.nx + kBlockX - 1) / kBlockX, g.ny, g.nz); }
+
+template <int Q, int ST, bool MASK, int ARITH>
+int launch_fused(const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
+                 const uint8_t* types, cudaStream_t st) {
+    using T = typename Store<ST>::T;
+    nat_fused_k<Q, ST, MASK, ARITH><<<cell_grid(g), kBlockX, 0, st>>>(g, cp, np, (const T*)src, (T*)dst, types);
+    return (int)cudaGetLastError();
+}
+
+template <int Q, int ST, bool MASK, int ARITH>
+int launch_raw(const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
+               const float* rho, const float* u, const uint8_t* types, cudaStream_t st) {
+    using T = typename Store<ST>::T;
+    nat_collide_raw_k<Q, ST, MASK, ARITH><<<cell_grid(g), kBlockX, 0, st>>>(g, cp, np, (const T*)src, (T*)dst,
+                                                                            rho, u, types);
+    return (int)cudaGetLastError();
+}
+
+// storage x mask x arith expansion for one Q
+template <int Q>
+int fused_q(int storage, int arith, bool m, const Geo& g, const CollideParams& cp, const NativeParams& np,
+            const void* src, void* dst, const uint8_t* types, cudaStream_t st) {
+    if (storage == 1)
+        return m ? launch_fused<Q, 1, true, kArithFP32>(g, cp, np, src, dst, types, st)
+                 : launch_fused<Q, 1, false, kArithFP32>(g, cp, np, src, dst, types, st);
+    if (arith == kArithReference)
+        return m ? launch_fused<Q, 0, true, kArithReference>(g, cp, np, src, dst, types, st)
+                 : launch_fused<Q, 0, false, kArithReference>(g, cp, np, src, dst, types, st);
+    return m ? launch_fused<Q, 0, true, kArithFP32>(g, cp, np, src, dst, types, st)
+             : launch_fused<Q, 0, false, kArithFP32>(g, cp, np, src, dst, types, st);
+}
+
+template <int Q>
+int raw_q(int storage, int arith, bool m, const Geo& g, const CollideParams& cp, const NativeParams& np,
+          const void* src, void* dst, const float* rho, const float* u, const uint8_t* types, cudaStream_t st) {
+    if (storage == 1)
+        return m ? launch_raw<Q, 1, true, kArithFP32>(g, cp, np, src, dst, rho, u, types, st)
+                 : launch_raw<Q, 1, false, kArithFP32>(g, cp, np, src, dst, rho, u, types, st);
+    if (arith == kArithReference)
+        return m ? launch_raw<Q, 0, true, kArithReference>(g, cp, np, src, dst, rho, u, types, st)
+                 : launch_raw<Q, 0, false, kArithReference>(g, cp, np, src, dst, rho, u, types, st);
+    return m ? launch_raw<Q, 0, true, kArithFP32>(g, cp, np, src, dst, rho, u, types, st)
+             : launch_raw<Q, 0, false, kArithFP32>(g, cp, np, src, dst, rho, u, types, st);
+}
+
+template <int Q, int ST, bool MASK>
+int launch_gather(const Geo& g, const NativeParams& np, const void* src, void* n_out, float* rho, float* u,
+                  const uint8_t* types, cudaStream_t st) {
+    using T = typename Store<ST>::T;
+    nat_gather_k<Q, ST, MASK><<<cell_grid(g), kBlockX, 0, st>>>(g, np, (const T*)src, (T*)n_out, rho, u, types);
+    return (int)cudaGetLastError();
+}
+
+template <int Q>
+int gather_q(int storage, bool m, const Geo& g, const NativeParams& np, const void* src, void* n_out, float* rho,
+             float* u, const uint8_t* types, cudaStream_t st) {
+    if (storage == 1)
+        return m ? launch_gather<Q, 1, true>(g, np, src, n_out, rho, u, types, st)
+                 : launch_gather<Q, 1, false>(g, np, src, n_out, rho, u, types, st);
+    return m ? launch_gather<Q, 0, true>(g, np, src, n_out, rho, u, types, st)
+             : launch_gather<Q, 0, false>(g, np, src, n_out, rho, u, types, st);
+}
+
+}  // namespace
+
+#define PLB_Q_DISPATCH(q, CALL) \
+    ((q) == 9 ? CALL(9) : (q) == 19 ? CALL(19) : (q) == 27 ? CALL(27) : (int)cudaErrorInvalidValue)
+
+int nat_fused_step(int q, int storage, int arith, bool has_mask, const Geo& g, const CollideParams& cp,
+                   const NativeParams& np, const void* src, void* dst, const uint8_t* types, cudaStream_t st) {
+#define CALL(Q) fused_q<Q>(storage, arith, has_mask, g, cp, np, src, dst, types, st)
+    return PLB_Q_DISPATCH(q, CALL);
+#undef CALL
+}
+
+int nat_collide_raw(int q, int storage, int arith, bool has_mask, const Geo& g, const CollideParams& cp,
+                    const NativeParams& np, const void* src, void* dst, const float* rho, const float* u,
+                    const uint8_t* types, cudaStream_t st) {
+#define CALL(Q) raw_q<Q>(storage, arith, has_mask, g, cp, np, src, dst, rho, u, types, st)
+    return PLB_Q_DISPATCH(q, CALL);
+#undef CALL
+}
+
+int nat_gather(int q, int storage, bool has_mask, const Geo& g, const NativeParams& np, const void* src,
+               void* n_out, float* rho, float* u, const uint8_t* types, cudaStream_t st) {
+#define CALL(Q) gather_q<Q>(storage, has_mask, g, np, src, n_out, rho, u, types, st)
+    return PLB_Q_DISPATCH(q, CALL);
+#undef CALL
+}
+
+int nat_reset_fields(const Geo& g, const NativeParams& np, const uint8_t* types, float* rho, float* u,
+                     cudaStream_t st) {
+    nat_reset_fields_k<<<cell_grid(g), kBlockX, 0, st>>>(g, np, types, rho, u);
+    return (int)cudaGetLastError();
+}
+
+int nat_build_types(int q, const Geo& g, const uint8_t* mask, int noslip_mask, uint8_t* scratch,
+                    uint8_t* types, cudaStream_t st) {
+#define CALL(Q) (nat_types_solid_k<Q><<<cell_grid(g), kBlockX, 0, st>>>(g, mask, noslip_mask, scratch), \
+                 nat_types_near_k<Q><<<cell_grid(g), kBlockX, 0, st>>>(g, scratch, types), (int)cudaGetLastError())
+    return PLB_Q_DISPATCH(q, CALL);
+#undef CALL
+}
+
+}  // namespace plb
