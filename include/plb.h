@@ -190,6 +190,26 @@ int plb_set_field(plb_solve* s, int32_t which, const float* in);
  * plbpd has no conservation diagnostics. */
 int plb_conservation(plb_solve* s, double* out4);
 
+/* The same FP64 sums for callers that cannot allocate device memory: a
+ * process that may not call cudaMalloc once it runs (its own memory pool, a
+ * hard memory quota, an allocator that must see every allocation) cannot use
+ * plb_conservation, whose solve handle allocates scratch.  This entry point
+ * allocates nothing.  No counterpart in plbpd, which has no conservation
+ * diagnostics.
+ *   n      device pointer, q planes of FP32 populations, plane k at
+ *          n + k*plane_stride, cells 0..ncells-1 contiguous in each plane
+ *   solid  device pointer to ncells bytes (nonzero = skip the cell), or NULL
+ *   out4   device pointer to 4 doubles: mass, momentum x, y, z
+ *   stream a cudaStream_t (NULL = legacy default stream); the call only
+ *          enqueues work, synchronize before reading out4
+ * Block partials live in a fixed 128 KiB __device__ array inside the library,
+ * so ncells is limited to 16,777,216 (PLB_EINVAL beyond).  The first call on
+ * a device looks that array's address up (cudaGetSymbolAddress, with the
+ * device current); make that first call before any stream capture.  All calls
+ * share the array: calls whose kernels overlap on the GPU race on it. */
+int plb_conservation_static(int32_t q, const float* n, int64_t ncells, int64_t plane_stride,
+                            const uint8_t* solid, double* out4, void* stream);
+
 /* Pinned host memory for fast transfers (cudaHostAlloc / cudaFreeHost). */
 int plb_host_alloc(size_t bytes, void** out);
 int plb_host_free(void* p);

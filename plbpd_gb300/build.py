@@ -21,7 +21,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libplb_gb300.so")
-SOURCES = ["capi.cu", "kernels_ref.cu", "kernels_native.cu", "kernels_util.cu"]
+SOURCES = ["capi.cu", "kernels_ref.cu", "kernels_native.cu", "kernels_util.cu", "kernels_static.cu"]
 HEADERS = ["lattice.cuh", "engine.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -65,6 +65,8 @@ _SIGS = [
     ("plb_get_field", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     ("plb_set_field", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     ("plb_conservation", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("plb_conservation_static", C.c_int, [C.c_int32, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
+                                          C.c_void_p]),
     ("plb_host_alloc", C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
     ("plb_host_free", C.c_int, [C.c_void_p]),
     ("plb_device_bytes", C.c_int64, [C.c_void_p]),

@@ -94,6 +94,8 @@ int graph_steps_default() {
 
 }  // namespace
 
+void plb::record_error(const std::string& msg) { g_last_error = msg; }
+
 // ---------------------------------------------------------------------------
 struct plb_solve {
     plb_params p;

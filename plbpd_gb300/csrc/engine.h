@@ -2,11 +2,15 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "lattice.cuh"
 
 namespace plb {
+
+// Stores the message plb_last_error() returns on this thread.
+void record_error(const std::string& msg);
 
 // Boundary description handed to the REFERENCE-semantics kernels.  Faces are
 // numbered east, west, north, south, up, down (plbpd's src/Boundary.cpp:17-18).
