@@ -73,9 +73,12 @@ extern "C" {
 #define PLB_ARITH_FP32 1
 
 /* Population storage.  FP16_DEV keeps f_k - w_k in IEEE half precision and
- * does all collision arithmetic in FP32 (NATIVE semantics only).          */
+ * does all collision arithmetic in FP32 (NATIVE semantics only).  FP64
+ * keeps populations and arithmetic in double: the reference run that
+ * reduced-precision runs are measured against (NATIVE semantics only).    */
 #define PLB_STORAGE_FP32 0
 #define PLB_STORAGE_FP16_DEV 1
+#define PLB_STORAGE_FP64 2
 
 /* Field ids: plbpd's SimData members n, ntmp, rho, u (src/SimData.hpp:18-21). */
 #define PLB_FIELD_N 0
@@ -133,6 +136,17 @@ int plb_relaxation(float nu, float* tau, float* omega);
  * (src/PLBPD.cpp:6-14).  Fields start as plbpd's do: n, ntmp, rho, u = 0. */
 int plb_solve_create(const plb_params* params, plb_solve** out);
 int plb_solve_destroy(plb_solve* s);
+
+/* Replace the collision parameters of an existing solve.  plbpd configures
+ * CollisionSRT from a Domain (src/CollisionSRT.cpp:14-21) independently of
+ * the SimData it is applied to; this call lets one device state be driven by
+ * whichever operator objects the caller applies to it. */
+int plb_set_relaxation(plb_solve* s, float nu, const float* force3);
+/* Replace the boundary description of an existing solve (REFERENCE
+ * semantics), as constructing another Boundary (src/Boundary.cpp:20-32) and
+ * applying it to the same SimData would.  Arguments as in plb_params. */
+int plb_set_boundary(plb_solve* s, float rho_solid, const int32_t* face_type6, const int32_t* face_has_vel6,
+                     const float* face_vel18);
 
 /* Obstacle mask, nz*ny*nx bytes with x fastest, nonzero = solid.  NATIVE
  * semantics only (plbpd has no obstacle masks; its wall rule,

@@ -30,6 +30,7 @@ struct orc_sim {
     void *n, *ntmp, *rho, *u;
     uint8_t* solid;       /* per node of the halo box: 1 = solid      */
     uint8_t* solid_vel;   /* 0..5 = wall face, 6 = obstacle           */
+    float* drho;          /* FP16 deviation arithmetic: sum of d_k    */
 };
 
 /* ---- lattice tables: src/LBModel.cpp:23-165 ------------------------------ */
@@ -114,6 +115,30 @@ static void orc_face_extent(const orc_sim* s, int f, long* e) {
 static const float kZeroVel[3] = {0.0f, 0.0f, 0.0f};
 static inline const float* orc_solid_velocity(const orc_sim* s, uint8_t v) {
     return v < 6 ? s->face_vel[v] : kZeroVel;
+}
+
+/* IEEE binary16 rounding, from the format's definition: 10 fraction bits,
+ * exponent range -14..15, subnormal quantum 2^-24, round half to even. */
+float orc_round_half(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    const uint32_t sign = u & 0x80000000u;
+    uint32_t a = u & 0x7fffffffu;
+    if (a >= 0x7f800000u) return f;                          /* inf, nan */
+    if (a < 0x38800000u) {                                   /* below 2^-14: fixed quantum */
+        float v;
+        memcpy(&v, &a, 4);
+        v = nearbyintf(v * 16777216.0f) * (1.0f / 16777216.0f);
+        memcpy(&a, &v, 4);
+    } else {
+        a += 0x00000fffu + ((a >> 13) & 1u);                 /* round the 13 dropped bits */
+        a &= ~0x00001fffu;
+        if (a >= 0x47800000u) a = 0x7f800000u;               /* beyond 65504: inf */
+    }
+    a |= sign;
+    float r;
+    memcpy(&r, &a, 4);
+    return r;
 }
 
 /* ---- two instantiations ----------------------------------------------------- */
@@ -218,7 +243,8 @@ orc_sim* orc_create(int q, long nx, long ny, long nz, float nu, float rho0,
     s->u = calloc(cells * 3, rs);
     s->solid = (uint8_t*)calloc(cells, 1);
     s->solid_vel = (uint8_t*)calloc(cells, 1);
-    if (!s->n || !s->ntmp || !s->rho || !s->u || !s->solid || !s->solid_vel) {
+    s->drho = (float*)calloc(cells, sizeof(float));
+    if (!s->n || !s->ntmp || !s->rho || !s->u || !s->solid || !s->solid_vel || !s->drho) {
         orc_destroy(s);
         return NULL;
     }
@@ -229,7 +255,7 @@ orc_sim* orc_create(int q, long nx, long ny, long nz, float nu, float rho0,
 void orc_destroy(orc_sim* s) {
     if (!s) return;
     free(s->n); free(s->ntmp); free(s->rho); free(s->u);
-    free(s->solid); free(s->solid_vel);
+    free(s->solid); free(s->solid_vel); free(s->drho);
     free(s);
 }
 
@@ -256,6 +282,7 @@ ORC_DISPATCH(noslip)
 ORC_DISPATCH(periodic)
 ORC_DISPATCH(moments)
 ORC_DISPATCH(reset)
+ORC_DISPATCH(quantize)
 
 void orc_initialize(orc_sim* s) {       /* PLBPD::initialize (src/PLBPD.cpp:16-19) */
     if (s->precision) init_fields_d(s); else init_fields_f(s);
@@ -267,6 +294,7 @@ void orc_step(orc_sim* s, long nsteps) {  /* src/PLBPD.cpp:23-30 */
         orc_collide(s);
         orc_stream(s);
         orc_noslip(s);
+        orc_quantize(s);
         orc_periodic(s);
         orc_moments(s);
         orc_reset(s);
@@ -293,9 +321,18 @@ static void* orc_field_ptr(const orc_sim* s, int which) {
     }
 }
 
+static int orc_fp16_pop(const orc_sim* s, int which) {
+    return !s->precision && s->arith == ORC_ARITH_FP16DEV && (which == ORC_N || which == ORC_NTMP);
+}
+
 void orc_get_field(const orc_sim* s, int which, float* out) {
     const size_t len = orc_field_len(s, which);
     const void* p = orc_field_ptr(s, which);
+    if (orc_fp16_pop(s, which)) {   /* populations are w + d */
+        const float* d = (const float*)p;
+        for (size_t i = 0; i < len; ++i) out[i] = d[i] + s->w[i % (size_t)s->q];
+        return;
+    }
     if (s->precision) {
         const double* d = (const double*)p;
         for (size_t i = 0; i < len; ++i) out[i] = (float)d[i];
@@ -307,6 +344,13 @@ void orc_get_field(const orc_sim* s, int which, float* out) {
 void orc_set_field(orc_sim* s, int which, const float* in) {
     const size_t len = orc_field_len(s, which);
     void* p = orc_field_ptr(s, which);
+    if (orc_fp16_pop(s, which)) {
+        float* d = (float*)p;
+        for (size_t i = 0; i < len; ++i) d[i] = orc_round_half(in[i] - s->w[i % (size_t)s->q]);
+        return;
+    }
+    if (!s->precision && which == ORC_RHO)
+        for (size_t i = 0; i < len; ++i) s->drho[i] = in[i] - 1.0f;
     if (s->precision) {
         double* d = (double*)p;
         for (size_t i = 0; i < len; ++i) d[i] = (double)in[i];

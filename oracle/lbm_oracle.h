@@ -43,7 +43,13 @@ enum { ORC_MODE_REFERENCE = 0, ORC_MODE_NATIVE = 1 };
  *   ORC_ARITH_AVX2    FP32 8-wide body + FP64 tail (src/CollisionSRT.cpp:93-148)
  *   ORC_ARITH_SCALAR  FP64 bracket for every direction (src/CollisionSRT.cpp:151-176)
  *   ORC_ARITH_FP32    the FP32 body's sequence for every direction          */
-enum { ORC_ARITH_AVX2 = 0, ORC_ARITH_SCALAR = 1, ORC_ARITH_FP32 = 2 };
+enum { ORC_ARITH_AVX2 = 0, ORC_ARITH_SCALAR = 1, ORC_ARITH_FP32 = 2,
+       /* ORC_MODE_NATIVE, float: populations held as deviations d = f - w
+        * rounded to IEEE binary16 after every step, moments and collision in
+        * FP32 in deviation form (the engine's FP16 storage):
+        *   drho = sum d_k, rho = 1 + drho, u = (sum c_k d_k) / rho,
+        *   d'_k = (1-omega) d_k + omega w_k (drho + rho (3cu + 4.5cu^2 - 1.5usq)) */
+       ORC_ARITH_FP16DEV = 3 };
 enum { ORC_FACE_NONE = 0, ORC_FACE_PERIODIC = 1, ORC_FACE_NOSLIP = 2 };
 /* field ids */
 enum { ORC_N = 0, ORC_NTMP = 1, ORC_RHO = 2, ORC_U = 3 };
@@ -88,6 +94,10 @@ void orc_set_field_f64(orc_sim* s, int which, const double* in);
 
 /* tau and omega as the reference derives them (src/CollisionSRT.cpp:19-20). */
 void orc_relaxation(const orc_sim* s, float* tau, float* omega);
+
+/* Nearest IEEE binary16 value of f (round to nearest even; overflow to inf),
+ * returned as a float. */
+float orc_round_half(float f);
 
 /* Sum over fluid interior nodes of n_k and n_k c_k, in double:
  * out[0] = mass, out[1..3] = momentum. */

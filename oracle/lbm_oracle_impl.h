@@ -11,9 +11,10 @@
 /* ---- collision, one node ------------------------------------------------ */
 /* CollisionSRT::_get_updated_u (src/CollisionSRT.cpp:71-81), _get_cu (:83-91),
  * _collision_kernel_avx2 (:93-148), _collision_kernel (:151-176). */
-static void FN(collide_node)(const orc_sim* s, R* nl, R rho, const R* ul) {
+static void FN(collide_node)(const orc_sim* s, R* nl, R rho, const R* ul, R drho) {
     const int q = s->q;
 #if ORC_IS_DOUBLE
+    (void)drho;
     const double tau = (double)s->tau;
     const double omega = 1.0 / tau;
     const double trho = tau / rho;
@@ -37,6 +38,18 @@ static void FN(collide_node)(const orc_sim* s, R* nl, R rho, const R* ul) {
     for (int k = 1; k < q; ++k)
         cu[k] = (float)s->c[k][0] * uu[0] + (float)s->c[k][1] * uu[1] +
                 (float)s->c[k][2] * uu[2];
+    if (s->arith == ORC_ARITH_FP16DEV) {
+        /* deviation form: nl holds d = f - w */
+        const float kusq16 = -1.5f * usq;
+        for (int k = 0; k < q; ++k) {
+            float t = fmaf(4.5f, cu[k] * cu[k], kusq16);
+            t = fmaf(3.0f, cu[k], t);
+            float e = fmaf(rho, t, drho);
+            e = s->w[k] * e;
+            nl[k] = fmaf(1.0f - omega, nl[k], omega * e);
+        }
+        return;
+    }
     int nbody;
     if (s->arith == ORC_ARITH_AVX2) nbody = (q / 8) * 8;
     else if (s->arith == ORC_ARITH_FP32) nbody = q;
@@ -76,6 +89,7 @@ static void FN(collide)(orc_sim* s) {
     R* n = (R*)s->n;
     const R* rho = (const R*)s->rho;
     const R* u = (const R*)s->u;
+    const float* drho = s->drho;
     const int q = s->q;
 #pragma omp parallel for schedule(static)
     for (long z = 1; z <= s->nz; ++z)
@@ -83,8 +97,28 @@ static void FN(collide)(orc_sim* s) {
             for (long x = 1; x <= s->nx; ++x) {
                 const size_t i = FN(node)(s, z, y, x);
                 if (s->mode == ORC_MODE_NATIVE && s->solid[i]) continue;
-                FN(collide_node)(s, n + i * q, rho[i], u + 3 * i);
+                FN(collide_node)(s, n + i * q, rho[i], u + 3 * i, (R)drho[i]);
             }
+}
+
+/* FP16 storage: every fluid population rounds to binary16 once per step,
+ * after the bounce-back writes (the engine rounds when it stores). */
+static void FN(quantize)(orc_sim* s) {
+#if ORC_IS_DOUBLE
+    (void)s;
+#else
+    if (s->arith != ORC_ARITH_FP16DEV) return;
+    float* n = (float*)s->n;
+    const int q = s->q;
+#pragma omp parallel for schedule(static)
+    for (long z = 1; z <= s->nz; ++z)
+        for (long y = 1; y <= s->ny; ++y)
+            for (long x = 1; x <= s->nx; ++x) {
+                const size_t i = FN(node)(s, z, y, x);
+                if (s->solid[i]) continue;
+                for (int k = 0; k < q; ++k) n[i * q + k] = orc_round_half(n[i * q + k]);
+            }
+#endif
 }
 
 /* Streaming::_push_kernel / _push_tbb (src/Streaming.cpp:62-94):
@@ -242,6 +276,12 @@ static void FN(moments)(orc_sim* s) {
                     uy += nk * (R)s->c[k][1];
                     uz += nk * (R)s->c[k][2];
                 }
+#if !ORC_IS_DOUBLE
+                if (s->arith == ORC_ARITH_FP16DEV) {   /* r is the density deviation */
+                    s->drho[i] = r;
+                    r = 1.0f + r;
+                }
+#endif
                 const R rinv = (R)1 / r;
                 rho[i] = r;
                 u[3 * i + 0] = ux * rinv;
@@ -311,8 +351,11 @@ static void FN(init_fields)(orc_sim* s) {
     }
 #else
     orc_eqlb(s->q, s->rho0, s->u0, feq);
+    if (s->arith == ORC_ARITH_FP16DEV)
+        for (int k = 0; k < s->q; ++k) feq[k] = orc_round_half(feq[k] - s->w[k]);
 #endif
     for (size_t i = 0; i < cells; ++i) {
+        s->drho[i] = s->rho0 - 1.0f;
         rho[i] = (R)s->rho0;
         for (int d = 0; d < 3; ++d) u[3 * i + d] = (R)s->u0[d];
         for (int k = 0; k < s->q; ++k) {
@@ -331,7 +374,8 @@ static void FN(conservation)(const orc_sim* s, double* out) {
                 const size_t i = FN(node)(s, z, y, x);
                 if (s->solid[i]) continue;
                 for (int k = 0; k < s->q; ++k) {
-                    const double v = (double)n[i * s->q + k];
+                    double v = (double)n[i * s->q + k];
+                    if (s->arith == ORC_ARITH_FP16DEV && !ORC_IS_DOUBLE) v += (double)s->w[k];
                     m += v;
                     px += v * s->c[k][0];
                     py += v * s->c[k][1];

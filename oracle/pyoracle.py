@@ -27,7 +27,7 @@ REF_DIR = os.path.join(HERE, "_ref")
 FACES = ("east", "west", "north", "south", "up", "down")
 FACE_NONE, FACE_PERIODIC, FACE_NOSLIP = 0, 1, 2
 MODE_REFERENCE, MODE_NATIVE = 0, 1
-ARITH_AVX2, ARITH_SCALAR, ARITH_FP32 = 0, 1, 2
+ARITH_AVX2, ARITH_SCALAR, ARITH_FP32, ARITH_FP16DEV = 0, 1, 2, 3
 N, NTMP, RHO, U = 0, 1, 2, 3
 Q_OF = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27}
 

@@ -21,8 +21,10 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libplb_gb300.so")
-SOURCES = ["capi.cu", "kernels_ref.cu", "kernels_native.cu", "kernels_util.cu", "kernels_static.cu"]
+SOURCES = ["capi.cu", "kernels_ref.cu", "kernels_native.cu", "kernels_util.cu", "kernels_static.cu", "facade.cpp"]
 HEADERS = ["lattice.cuh", "engine.h"]
+FACADE_HEADERS = ["Boundary.hpp", "CalcMoments.hpp", "Collision.hpp", "CollisionSRT.hpp", "Domain.hpp", "EqlbDist.hpp",
+                  "Field.hpp", "Flow.hpp", "LBDynamics.hpp", "LBModel.hpp", "PLBPD.hpp", "SimData.hpp", "Streaming.hpp"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
@@ -44,6 +46,9 @@ def _stamp() -> str:
             h.update(f.read())
     with open(os.path.join(ROOT, "include", "plb.h"), "rb") as f:
         h.update(f.read())
+    for name in FACADE_HEADERS:
+        with open(os.path.join(ROOT, "include", "plbpd", name), "rb") as f:
+            h.update(f.read())
     h.update(" ".join(NVCC_FLAGS).encode())
     h.update(os.uname().machine.encode())
     return h.hexdigest()
@@ -61,7 +66,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cc = nvcc()
 
     def compile_one(src: str) -> str:
-        obj = os.path.join(OUT, src.replace(".cu", ".o"))
+        obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
         cmd = [cc] + NVCC_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -19,7 +19,7 @@ FACE_NONE, FACE_PERIODIC, FACE_NOSLIP = 0, 1, 2
 FACES = ("east", "west", "north", "south", "up", "down")
 SEMANTICS_REFERENCE, SEMANTICS_NATIVE = 0, 1
 ARITH_REFERENCE, ARITH_FP32 = 0, 1
-STORAGE_FP32, STORAGE_FP16_DEV = 0, 1
+STORAGE_FP32, STORAGE_FP16_DEV, STORAGE_FP64 = 0, 1, 2
 FIELD_N, FIELD_NTMP, FIELD_RHO, FIELD_U = 0, 1, 2, 3
 Q_OF = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27}
 
@@ -47,6 +47,8 @@ _SIGS = [
     ("plb_relaxation", C.c_int, [C.c_float, C.c_void_p, C.c_void_p]),
     ("plb_solve_create", C.c_int, [C.POINTER(Params), C.POINTER(C.c_void_p)]),
     ("plb_solve_destroy", C.c_int, [C.c_void_p]),
+    ("plb_set_relaxation", C.c_int, [C.c_void_p, C.c_float, C.c_void_p]),
+    ("plb_set_boundary", C.c_int, [C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("plb_set_mask", C.c_int, [C.c_void_p, C.c_void_p]),
     ("plb_initialize", C.c_int, [C.c_void_p]),
     ("plb_step", C.c_int, [C.c_void_p, C.c_int64]),

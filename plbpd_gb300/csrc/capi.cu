@@ -170,6 +170,59 @@ void release(plb_solve* s) {
     delete s;
 }
 
+// CollisionSRT's parameters (src/CollisionSRT.cpp:14-21).
+void set_collision_params(plb_solve* s, float nu, const float* force) {
+    s->p.nu = nu;
+    relaxation(nu, &s->cp.tau, &s->cp.omega);
+    s->cp.omc = 1.0f - s->cp.omega;
+    s->cp.fx = force[0]; s->cp.fy = force[1]; s->cp.fz = force[2];
+    for (int i = 0; i < 3; ++i) s->p.force[i] = force[i];
+}
+
+// Boundary's parameters (src/Boundary.cpp:20-32) and the no-slip launch
+// groups: faces in plbpd's order; two parallel faces share a launch when they
+// are far enough apart not to touch the same slots.
+void set_face_params(plb_solve* s, float rho_solid, const int32_t* face_type, const int32_t* face_has_vel,
+                     const float* face_vel) {
+    const float cs2 = (float)(1. / 3.);
+    const float cs2inv = 1.0f / cs2;   // src/Boundary.cpp:27
+    s->fp.noslip_mask = 0; s->fp.vel_mask = 0;
+    for (int f = 0; f < 6; ++f) {
+        s->p.face_type[f] = face_type[f];
+        s->p.face_has_vel[f] = face_has_vel[f];
+        if (face_type[f] == PLB_FACE_NOSLIP) s->fp.noslip_mask |= 1 << f;
+        if (face_has_vel[f]) s->fp.vel_mask |= 1 << f;
+        for (int i = 0; i < 3; ++i) {
+            s->fp.vel[f][i] = face_has_vel[f] ? face_vel[3 * f + i] : 0.0f;
+            s->p.face_vel[f][i] = s->fp.vel[f][i];
+        }
+    }
+    s->p.rho_solid = rho_solid;
+    s->fp.rho_solid = rho_solid;
+    s->fp.cs2inv = cs2inv;
+    s->fp.ew_periodic = face_type[0] == PLB_FACE_PERIODIC && face_type[1] == PLB_FACE_PERIODIC;
+    s->fp.ns_periodic = face_type[2] == PLB_FACE_PERIODIC && face_type[3] == PLB_FACE_PERIODIC;
+    std::memset(&s->np, 0, sizeof(s->np));
+    for (int f = 0; f < 6; ++f)
+        for (int i = 0; i < 3; ++i) s->np.vel[f][i] = s->fp.vel[f][i];
+    s->np.rho_solid = rho_solid;
+    s->np.cs2inv = cs2inv;
+    const long long ext[3] = {s->p.nx, s->p.ny, s->p.nz};
+    s->ngroups = 0;
+    int f = 0;
+    while (f < 6) {
+        if (!((s->fp.noslip_mask >> f) & 1)) { ++f; continue; }
+        const int axis = f / 2;
+        if ((f % 2) == 0 && ((s->fp.noslip_mask >> (f + 1)) & 1) && ext[axis] >= 4) {
+            s->groups[s->ngroups][0] = f; s->groups[s->ngroups][1] = f + 1; s->group_len[s->ngroups++] = 2;
+            f += 2;
+        } else {
+            s->groups[s->ngroups][0] = f; s->group_len[s->ngroups++] = 1;
+            f += 1;
+        }
+    }
+}
+
 int validate(const plb_params* p) {
     if (!p) return fail(PLB_EINVAL, "params is null");
     if (p->q != 9 && p->q != 19 && p->q != 27)
@@ -180,17 +233,19 @@ int validate(const plb_params* p) {
     for (int f = 0; f < 6; ++f) {
         if (p->face_type[f] < PLB_FACE_NONE || p->face_type[f] > PLB_FACE_NOSLIP)
             return fail(PLB_EINVAL, "invalid face type");
-        // src/Boundary.cpp:197 reads the velocity of every no-slip face
-        if (p->face_type[f] == PLB_FACE_NOSLIP && !p->face_has_vel[f])
+        // a NATIVE wall moves with its face velocity, so it needs one; under
+        // REFERENCE semantics the lookup fails only when no-slip runs
+        // (src/Boundary.cpp:197), which plb_apply_noslip and plb_step check
+        if (p->semantics == PLB_SEMANTICS_NATIVE && p->face_type[f] == PLB_FACE_NOSLIP && !p->face_has_vel[f])
             return fail(PLB_EINVAL, "no-slip face " + std::to_string(f) + " has no velocity entry");
     }
     if (p->semantics != PLB_SEMANTICS_REFERENCE && p->semantics != PLB_SEMANTICS_NATIVE)
         return fail(PLB_EINVAL, "invalid semantics");
     if (p->arith != PLB_ARITH_REFERENCE && p->arith != PLB_ARITH_FP32) return fail(PLB_EINVAL, "invalid arith");
-    if (p->storage != PLB_STORAGE_FP32 && p->storage != PLB_STORAGE_FP16_DEV)
+    if (p->storage != PLB_STORAGE_FP32 && p->storage != PLB_STORAGE_FP16_DEV && p->storage != PLB_STORAGE_FP64)
         return fail(PLB_EINVAL, "invalid storage");
-    if (p->storage == PLB_STORAGE_FP16_DEV && p->semantics != PLB_SEMANTICS_NATIVE)
-        return fail(PLB_EUNSUPPORTED, "FP16 storage needs NATIVE semantics");
+    if (p->storage != PLB_STORAGE_FP32 && p->semantics != PLB_SEMANTICS_NATIVE)
+        return fail(PLB_EUNSUPPORTED, "FP16 and FP64 storage need NATIVE semantics");
     if (p->semantics == PLB_SEMANTICS_NATIVE) {
         int32_t c[27 * 3];
         tables(p->q, c, nullptr, nullptr);
@@ -219,7 +274,20 @@ int ensure_staging(plb_solve* s) {
 }
 
 // ---- REFERENCE semantics ---------------------------------------------------
+// plbpd looks the wall velocity of every no-slip face up when no-slip runs
+// (src/Boundary.cpp:197) and throws if it is missing.
+int check_noslip_velocities(const plb_solve* s) {
+    const int missing = s->fp.noslip_mask & ~s->fp.vel_mask;
+    if (missing) {
+        int f = 0;
+        while (!((missing >> f) & 1)) ++f;
+        return fail(PLB_EINVAL, "no-slip face " + std::to_string(f) + " has no velocity entry");
+    }
+    return PLB_OK;
+}
+
 int ref_noslip_all(plb_solve* s) {
+    PLB_TRY(check_noslip_velocities(s));
     float* n = (float*)s->f[s->cur];
     for (int i = 0; i < s->ngroups; ++i)
         PLB_KERNEL(ref_noslip(s->q, s->g, s->fp, s->groups[i], s->group_len[i], n, s->rho, s->stream));
@@ -257,11 +325,20 @@ int nat_one_step(plb_solve* s) {
     return PLB_OK;
 }
 
-// POST -> RAW: n_t and its moments from P_{t-1}.
-int nat_materialize(plb_solve* s) {
-    if (!s->post) return PLB_OK;
+// n_t and its moments from P_{t-1}, into the other buffer and the fields;
+// the state itself is left as it is (POST stays POST), so reading the state
+// does not change the trajectory.
+int nat_gather_to_other(plb_solve* s) {
     PLB_KERNEL(nat_gather(s->q, s->storage, s->has_mask, s->g, s->np, s->f[s->cur], s->f[1 - s->cur], s->rho,
                           s->u, s->types, s->stream));
+    return PLB_OK;
+}
+
+// POST -> RAW: n_t and its moments become the state (before the caller
+// replaces part of it).
+int nat_materialize(plb_solve* s) {
+    if (!s->post) return PLB_OK;
+    PLB_TRY(nat_gather_to_other(s));
     s->cur = 1 - s->cur;
     s->post = false;
     return PLB_OK;
@@ -297,6 +374,7 @@ int march(plb_solve* s, int64_t n) {
     if (n == 0) return PLB_OK;
     const int64_t G = s->graph_steps;
     if (!s->native) {
+        PLB_TRY(check_noslip_velocities(s));
         // the first step reads the fields when they are the caller's; the
         // last writes every node back so the other buffer equals plbpd's ntmp
         int64_t done = 0;
@@ -378,7 +456,7 @@ int plb_solve_create(const plb_params* params, plb_solve** out) {
     // geometry
     Geo& g = s->g;
     g.nx = (int)params->nx; g.ny = (int)params->ny; g.nz = (int)params->nz;
-    const size_t esize = s->storage == PLB_STORAGE_FP16_DEV ? 2 : 4;
+    const size_t esize = s->storage == PLB_STORAGE_FP16_DEV ? 2 : s->storage == PLB_STORAGE_FP64 ? 8 : 4;
     if (s->native) {
         g.h = 0; g.xoff = 0;
         g.ys = round_up(g.nx, 32 / (long long)esize);
@@ -396,43 +474,8 @@ int plb_solve_create(const plb_params* params, plb_solve** out) {
         g.ks = round_up(g.fs, 64);
     }
     // collision and boundary parameters, derived as plbpd derives them
-    relaxation(params->nu, &s->cp.tau, &s->cp.omega);
-    s->cp.omc = 1.0f - s->cp.omega;
-    s->cp.fx = params->force[0]; s->cp.fy = params->force[1]; s->cp.fz = params->force[2];
-    const float cs2 = (float)(1. / 3.);
-    const float cs2inv = 1.0f / cs2;   // src/Boundary.cpp:27
-    s->fp.noslip_mask = 0; s->fp.vel_mask = 0;
-    for (int f = 0; f < 6; ++f) {
-        if (params->face_type[f] == PLB_FACE_NOSLIP) s->fp.noslip_mask |= 1 << f;
-        if (params->face_has_vel[f]) s->fp.vel_mask |= 1 << f;
-        for (int i = 0; i < 3; ++i) s->fp.vel[f][i] = params->face_has_vel[f] ? params->face_vel[f][i] : 0.0f;
-    }
-    s->fp.rho_solid = params->rho_solid;
-    s->fp.cs2inv = cs2inv;
-    s->fp.ew_periodic = params->face_type[0] == PLB_FACE_PERIODIC && params->face_type[1] == PLB_FACE_PERIODIC;
-    s->fp.ns_periodic = params->face_type[2] == PLB_FACE_PERIODIC && params->face_type[3] == PLB_FACE_PERIODIC;
-    std::memset(&s->np, 0, sizeof(s->np));
-    for (int f = 0; f < 6; ++f)
-        for (int i = 0; i < 3; ++i) s->np.vel[f][i] = s->fp.vel[f][i];
-    s->np.rho_solid = params->rho_solid;
-    s->np.cs2inv = cs2inv;
-    // no-slip launch groups: faces in plbpd's order; two parallel faces share
-    // a launch when they are far enough apart not to touch the same slots
-    {
-        const long long ext[3] = {params->nx, params->ny, params->nz};
-        int f = 0;
-        while (f < 6) {
-            if (!((s->fp.noslip_mask >> f) & 1)) { ++f; continue; }
-            const int axis = f / 2;
-            if ((f % 2) == 0 && ((s->fp.noslip_mask >> (f + 1)) & 1) && ext[axis] >= 4) {
-                s->groups[s->ngroups][0] = f; s->groups[s->ngroups][1] = f + 1; s->group_len[s->ngroups++] = 2;
-                f += 2;
-            } else {
-                s->groups[s->ngroups][0] = f; s->group_len[s->ngroups++] = 1;
-                f += 1;
-            }
-        }
-    }
+    set_collision_params(s, params->nu, params->force);
+    set_face_params(s, params->rho_solid, params->face_type, params->face_has_vel, &params->face_vel[0][0]);
     // device memory
     {
         const cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
@@ -491,6 +534,37 @@ int plb_solve_destroy(plb_solve* s) {
     return PLB_OK;
 }
 
+int plb_set_relaxation(plb_solve* s, float nu, const float* force3) {
+    if (!s || !force3) return fail(PLB_EINVAL, "null argument");
+    if (s->p.nu == nu && s->p.force[0] == force3[0] && s->p.force[1] == force3[1] && s->p.force[2] == force3[2])
+        return PLB_OK;
+    PLB_TRY(set_device(s));
+    PLB_TRY(sync(s));
+    set_collision_params(s, nu, force3);
+    drop_graphs(s);   // captured launches carry the old parameters
+    return PLB_OK;
+}
+
+int plb_set_boundary(plb_solve* s, float rho_solid, const int32_t* face_type6, const int32_t* face_has_vel6,
+                     const float* face_vel18) {
+    if (!s || !face_type6 || !face_has_vel6 || !face_vel18) return fail(PLB_EINVAL, "null argument");
+    if (s->native) return fail(PLB_EUNSUPPORTED, "changing the boundary needs REFERENCE semantics");
+    bool same = s->p.rho_solid == rho_solid;
+    for (int f = 0; f < 6; ++f) {
+        if (face_type6[f] < PLB_FACE_NONE || face_type6[f] > PLB_FACE_NOSLIP) return fail(PLB_EINVAL, "invalid face type");
+        same = same && s->p.face_type[f] == face_type6[f] && (s->p.face_has_vel[f] != 0) == (face_has_vel6[f] != 0);
+        for (int i = 0; i < 3; ++i)
+            same = same && (!face_has_vel6[f] || s->p.face_vel[f][i] == face_vel18[3 * f + i]);
+    }
+    if (same) return PLB_OK;
+    PLB_TRY(set_device(s));
+    PLB_TRY(sync(s));
+    PLB_TRY(ref_materialize_fields(s));   // the pending resets belong to the old boundary
+    set_face_params(s, rho_solid, face_type6, face_has_vel6, face_vel18);
+    drop_graphs(s);
+    return PLB_OK;
+}
+
 int plb_set_mask(plb_solve* s, const uint8_t* mask) {
     if (!s) return fail(PLB_EINVAL, "solve is null");
     if (!s->native) return fail(PLB_EUNSUPPORTED, "obstacle masks need NATIVE semantics");
@@ -509,9 +583,10 @@ int plb_set_mask(plb_solve* s, const uint8_t* mask) {
 int plb_initialize(plb_solve* s) {
     if (!s) return fail(PLB_EINVAL, "solve is null");
     PLB_TRY(set_device(s));
-    s->cur = 0;
-    PLB_KERNEL(util_init_uniform(s->q, s->storage, s->g, s->consts, s->p.rho0, s->p.u0, s->f[0], s->f[1], s->rho,
-                                 s->u, s->stream));
+    // Domain::initialize writes n, rho and u and leaves ntmp as it is
+    if (s->native) s->post = false;
+    PLB_KERNEL(util_init_uniform(s->q, s->storage, s->g, s->consts, s->p.rho0, s->p.u0, s->f[s->cur], nullptr,
+                                 s->rho, s->u, s->stream));
     if (s->native) {
         if (s->has_mask) PLB_KERNEL(nat_reset_fields(s->g, s->np, s->types, s->rho, s->u, s->stream));
         s->post = false;
@@ -616,16 +691,20 @@ int plb_get_field(plb_solve* s, int32_t which, float* out) {
     if (which < PLB_FIELD_N || which > PLB_FIELD_U) return fail(PLB_EINVAL, "invalid field id");
     PLB_TRY(set_device(s));
     const size_t len = plb_field_len(s, which);
+    int n_buf = s->cur;   // buffer that holds n for FIELD_N
     if (s->native) {
         if (which == PLB_FIELD_NTMP) { std::memset(out, 0, len * sizeof(float)); return PLB_OK; }
-        PLB_TRY(nat_materialize(s));
+        if (s->post) {
+            PLB_TRY(nat_gather_to_other(s));
+            n_buf = 1 - s->cur;
+        }
     } else if (which == PLB_FIELD_RHO || which == PLB_FIELD_U) {
         PLB_TRY(ref_materialize_fields(s));
     }
     PLB_TRY(ensure_staging(s));
     const float* wk = s->consts + s->q;
     if (which == PLB_FIELD_N || which == PLB_FIELD_NTMP) {
-        const void* src = s->f[which == PLB_FIELD_N ? s->cur : 1 - s->cur];
+        const void* src = s->f[which == PLB_FIELD_N ? n_buf : 1 - s->cur];
         PLB_KERNEL(util_export(s->storage, s->q, s->g, src, wk, s->staging, s->stream));
     } else {
         PLB_KERNEL(util_export(0, which == PLB_FIELD_RHO ? 1 : 3, s->g, which == PLB_FIELD_RHO ? s->rho : s->u,

@@ -13,8 +13,11 @@
 // with rho[x] the density node x collided with -- available in registers when
 // P[x][k] is stored, so the term is applied on the store side.
 //
-// Storage: FP32 populations, or FP16 deviations d_k = f_k - w_k with all
-// arithmetic in FP32 (the deviation form keeps the small part of f_k).
+// Storage (template parameter ST):
+//   0  FP32 populations, plbpd's FP32 arithmetic (or FP32-only, ARITH)
+//   1  FP16 deviations d_k = f_k - w_k, arithmetic in FP32 in deviation form
+//   2  FP64 populations and FP64 arithmetic: the reference run of the same
+//      method that reduced-precision runs are measured against
 #include "engine.h"
 
 namespace plb {
@@ -25,13 +28,23 @@ constexpr int kBlockX = 128;
 template <int ST> struct Store;
 template <> struct Store<0> {
     using T = float;
+    using R = float;
     __device__ static __forceinline__ float ld(const float* p, long long i) { return __ldg(p + i); }
     __device__ static __forceinline__ void st(float* p, long long i, float v) { __stcs(p + i, v); }
 };
 template <> struct Store<1> {
     using T = __half;
+    using R = float;
     __device__ static __forceinline__ float ld(const __half* p, long long i) { return __half2float(__ldg(p + i)); }
-    __device__ static __forceinline__ void st(__half* p, long long i, float v) { __stcs(reinterpret_cast<unsigned short*>(p) + i, __half_as_ushort(__float2half_rn(v))); }
+    __device__ static __forceinline__ void st(__half* p, long long i, float v) {
+        __stcs(reinterpret_cast<unsigned short*>(p) + i, __half_as_ushort(__float2half_rn(v)));
+    }
+};
+template <> struct Store<2> {
+    using T = double;
+    using R = double;
+    __device__ static __forceinline__ double ld(const double* p, long long i) { return __ldg(p + i); }
+    __device__ static __forceinline__ void st(double* p, long long i, double v) { __stcs(p + i, v); }
 };
 
 // Neighbour index helper: element offsets of x-1, x, x+1 (and y, z) with the
@@ -57,8 +70,8 @@ struct Nbr {
     }
 };
 
-// Collision in deviation form for FP16 storage.  d_k = f_k - w_k,
-// drho = sum d_k, rho = 1 + drho, and
+// ---- FP16 storage: deviation form -----------------------------------------
+// d_k = f_k - w_k, drho = sum d_k, rho = 1 + drho, and
 //   f_eq,k - w_k = w_k (drho + rho (3 cu + 4.5 cu^2 - 1.5 usq)),
 //   d'_k = (1 - omega) d_k + omega (f_eq,k - w_k).
 template <int Q>
@@ -81,8 +94,6 @@ __device__ __forceinline__ void collide_node_dev(float (&d)[Q], float drho, floa
     }
 }
 
-// Moments in deviation form: drho = sum d_k, j = sum c_k d_k,
-// u = j / (1 + drho).
 template <int Q>
 __device__ __forceinline__ void node_moments_dev(const float (&d)[Q], float& drho, float& rho, float& ux,
                                                  float& uy, float& uz) {
@@ -95,21 +106,128 @@ __device__ __forceinline__ void node_moments_dev(const float (&d)[Q], float& drh
     uz = __fmul_rn(jz, rinv);
 }
 
+// ---- FP64 storage: the same method in double ---------------------------------
+// Op order: u_eq = u + F (tau/rho); usq = (ux^2 + uy^2) + uz^2;
+// neq = (w rho)(((1 + 3cu) + (4.5cu)cu) - 1.5usq); n = (1-omega) n + omega neq.
+template <int Q>
+__device__ __forceinline__ double dot_c_d(int k, double ux, double uy, double uz) {
+    double acc = 0.0;
+    bool any = false;
+    if (Lattice<Q>::cx(k) != 0) { acc = Lattice<Q>::cx(k) > 0 ? ux : -ux; any = true; }
+    if (Lattice<Q>::cy(k) != 0) {
+        const double t = Lattice<Q>::cy(k) > 0 ? uy : -uy;
+        acc = any ? __dadd_rn(acc, t) : t;
+        any = true;
+    }
+    if (Lattice<Q>::cz(k) != 0) {
+        const double t = Lattice<Q>::cz(k) > 0 ? uz : -uz;
+        acc = any ? __dadd_rn(acc, t) : t;
+    }
+    return acc;
+}
+
+template <int Q>
+__device__ __forceinline__ void node_moments_d(const double (&f)[Q], double& rho, double& ux, double& uy,
+                                               double& uz) {
+    double r = 0.0, jx = 0.0, jy = 0.0, jz = 0.0;
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        r = __dadd_rn(r, f[k]);
+        if (Lattice<Q>::cx(k) > 0) jx = __dadd_rn(jx, f[k]);
+        if (Lattice<Q>::cx(k) < 0) jx = __dsub_rn(jx, f[k]);
+        if (Lattice<Q>::cy(k) > 0) jy = __dadd_rn(jy, f[k]);
+        if (Lattice<Q>::cy(k) < 0) jy = __dsub_rn(jy, f[k]);
+        if (Lattice<Q>::cz(k) > 0) jz = __dadd_rn(jz, f[k]);
+        if (Lattice<Q>::cz(k) < 0) jz = __dsub_rn(jz, f[k]);
+    }
+    const double rinv = __ddiv_rn(1.0, r);
+    rho = r;
+    ux = __dmul_rn(jx, rinv);
+    uy = __dmul_rn(jy, rinv);
+    uz = __dmul_rn(jz, rinv);
+}
+
+template <int Q>
+__device__ __forceinline__ void collide_node_d(double (&f)[Q], double rho, double ux, double uy, double uz,
+                                               const CollideParams& P) {
+    const double tau = (double)P.tau;
+    const double omega = __ddiv_rn(1.0, tau);
+    const double omc = __dsub_rn(1.0, omega);
+    const double tr = __ddiv_rn(tau, rho);
+    const double vx = __dadd_rn(ux, __dmul_rn((double)P.fx, tr));
+    const double vy = __dadd_rn(uy, __dmul_rn((double)P.fy, tr));
+    const double vz = __dadd_rn(uz, __dmul_rn((double)P.fz, tr));
+    const double usq = __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz));
+    const double k15 = __dmul_rn(1.5, usq);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        const double cu = (k == 0) ? 0.0 : dot_c_d<Q>(k, vx, vy, vz);
+        double br = __dadd_rn(1.0, __dmul_rn(3.0, cu));
+        br = __dadd_rn(br, __dmul_rn(__dmul_rn(4.5, cu), cu));
+        br = __dsub_rn(br, k15);
+        const double neq = __dmul_rn(__dmul_rn((double)weight<Q>(k), rho), br);
+        f[k] = __dadd_rn(__dmul_rn(omc, f[k]), __dmul_rn(omega, neq));
+    }
+}
+
+// ---- per storage: moments + collision, and the moving-wall correction ---------
+template <int Q, int ST, int ARITH>
+__device__ __forceinline__ void update_node(typename Store<ST>::R (&f)[Q], typename Store<ST>::R& rho,
+                                            const CollideParams& cp) {
+    if constexpr (ST == 0) {
+        float ux, uy, uz;
+        node_moments<Q>(f, rho, ux, uy, uz);
+        collide_node<Q, ARITH>(f, rho, ux, uy, uz, cp);
+    } else if constexpr (ST == 1) {
+        float drho, ux, uy, uz;
+        node_moments_dev<Q>(f, drho, rho, ux, uy, uz);
+        collide_node_dev<Q>(f, drho, rho, ux, uy, uz, cp);
+    } else {
+        double ux, uy, uz;
+        node_moments_d<Q>(f, rho, ux, uy, uz);
+        collide_node_d<Q>(f, rho, ux, uy, uz, cp);
+    }
+}
+
+template <int Q, int ST>
+__device__ __forceinline__ void moments_any(const typename Store<ST>::R (&f)[Q], typename Store<ST>::R& rho,
+                                            typename Store<ST>::R& ux, typename Store<ST>::R& uy,
+                                            typename Store<ST>::R& uz) {
+    if constexpr (ST == 0) node_moments<Q>(f, rho, ux, uy, uz);
+    else if constexpr (ST == 1) { float drho; node_moments_dev<Q>(f, drho, rho, ux, uy, uz); }
+    else node_moments_d<Q>(f, rho, ux, uy, uz);
+}
+
+// v - 2 w_k rho (c_k . u_b) / c_s^2, in the storage's arithmetic
+template <int Q, int ST>
+__device__ __forceinline__ typename Store<ST>::R wall_corrected(int k, typename Store<ST>::R v,
+                                                                typename Store<ST>::R rho, const float* ub,
+                                                                float cs2inv) {
+    if constexpr (ST == 2) {
+        const double cu = __dadd_rn(__dadd_rn(__dmul_rn((double)Lattice<Q>::cx(k), (double)ub[0]),
+                                              __dmul_rn((double)Lattice<Q>::cy(k), (double)ub[1])),
+                                    __dmul_rn((double)Lattice<Q>::cz(k), (double)ub[2]));
+        const double t = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(2.0, (double)weight<Q>(k)), rho), cu), (double)cs2inv);
+        return __dsub_rn(v, t);
+    } else {
+        return __fsub_rn(v, wall_term<Q>(k, rho, dot_c_full<Q>(k, ub), cs2inv));
+    }
+}
+
 // Stores the collided populations of a fluid node; a direction that points
 // into a solid node becomes the bounce-back slot and carries the moving-wall
 // term (src/Boundary.cpp:215-217).
 template <int Q, int ST, bool MASK>
 __device__ __forceinline__ void store_node(typename Store<ST>::T* __restrict__ dst, const Geo& g,
                                            const NativeParams& np, const uint8_t* __restrict__ types,
-                                           const Nbr& nb, long long node, bool near, float rho,
-                                           const float (&f)[Q]) {
+                                           const Nbr& nb, long long node, bool near, typename Store<ST>::R rho,
+                                           const typename Store<ST>::R (&f)[Q]) {
 #pragma unroll
     for (int k = 0; k < Q; ++k) {
-        float v = f[k];
+        typename Store<ST>::R v = f[k];
         if (MASK && near && k != 0) {
             const uint8_t t = __ldg(types + nb.at<Q>(k, +1));
-            if (t & kSolid)
-                v = __fsub_rn(v, wall_term<Q>(k, rho, dot_c_full<Q>(k, np.vel[t & kVelMask]), np.cs2inv));
+            if (t & kSolid) v = wall_corrected<Q, ST>(k, v, rho, np.vel[t & kVelMask], np.cs2inv);
         }
         Store<ST>::st(dst, k * g.ks + node, v);
     }
@@ -119,7 +237,7 @@ __device__ __forceinline__ void store_node(typename Store<ST>::T* __restrict__ d
 template <int Q, int ST, bool MASK>
 __device__ __forceinline__ void gather_node(const typename Store<ST>::T* __restrict__ src, const Geo& g,
                                             const uint8_t* __restrict__ types, const Nbr& nb,
-                                            long long node, bool near, float (&f)[Q]) {
+                                            long long node, bool near, typename Store<ST>::R (&f)[Q]) {
 #pragma unroll
     for (int k = 0; k < Q; ++k) {
         long long s = nb.at<Q>(k, -1);
@@ -136,6 +254,7 @@ template <int Q, int ST, bool MASK, int ARITH>
 __global__ void __launch_bounds__(kBlockX)
 nat_fused_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::T* __restrict__ src,
             typename Store<ST>::T* __restrict__ dst, const uint8_t* __restrict__ types) {
+    using R = typename Store<ST>::R;
     const int x = blockIdx.x * kBlockX + threadIdx.x;
     const int y = blockIdx.y, z = blockIdx.z;
     if (x >= g.nx) return;
@@ -147,18 +266,10 @@ nat_fused_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::
         near = (t & kNearSolid) != 0;
     }
     const Nbr nb(g, x, y, z);
-    float f[Q];
+    R f[Q];
     gather_node<Q, ST, MASK>(src, g, types, nb, node, near, f);
-    float rho;
-    if (ST == 0) {
-        float ux, uy, uz;
-        node_moments<Q>(f, rho, ux, uy, uz);
-        collide_node<Q, ARITH>(f, rho, ux, uy, uz, cp);
-    } else {
-        float drho, ux, uy, uz;
-        node_moments_dev<Q>(f, drho, rho, ux, uy, uz);
-        collide_node_dev<Q>(f, drho, rho, ux, uy, uz, cp);
-    }
+    R rho;
+    update_node<Q, ST, ARITH>(f, rho, cp);
     store_node<Q, ST, MASK>(dst, g, np, types, nb, node, near, rho, f);
 }
 
@@ -168,6 +279,7 @@ __global__ void __launch_bounds__(kBlockX)
 nat_collide_raw_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::T* __restrict__ src,
                   typename Store<ST>::T* __restrict__ dst, const float* __restrict__ rho_f,
                   const float* __restrict__ u_f, const uint8_t* __restrict__ types) {
+    using R = typename Store<ST>::R;
     const int x = blockIdx.x * kBlockX + threadIdx.x;
     const int y = blockIdx.y, z = blockIdx.z;
     if (x >= g.nx) return;
@@ -179,13 +291,14 @@ nat_collide_raw_k(Geo g, CollideParams cp, NativeParams np, const typename Store
         near = (t & kNearSolid) != 0;
     }
     const Nbr nb(g, x, y, z);
-    float f[Q];
+    R f[Q];
 #pragma unroll
     for (int k = 0; k < Q; ++k) f[k] = Store<ST>::ld(src, k * g.ks + node);
-    const float rho = rho_f[node];
-    const float ux = u_f[node], uy = u_f[g.ks + node], uz = u_f[2 * g.ks + node];
-    if (ST == 0) collide_node<Q, ARITH>(f, rho, ux, uy, uz, cp);
-    else collide_node_dev<Q>(f, __fsub_rn(rho, 1.0f), rho, ux, uy, uz, cp);
+    const R rho = (R)rho_f[node];
+    const R ux = (R)u_f[node], uy = (R)u_f[g.ks + node], uz = (R)u_f[2 * g.ks + node];
+    if constexpr (ST == 0) collide_node<Q, ARITH>(f, rho, ux, uy, uz, cp);
+    else if constexpr (ST == 1) collide_node_dev<Q>(f, __fsub_rn(rho, 1.0f), rho, ux, uy, uz, cp);
+    else collide_node_d<Q>(f, rho, ux, uy, uz, cp);
     store_node<Q, ST, MASK>(dst, g, np, types, nb, node, near, rho, f);
 }
 
@@ -196,6 +309,7 @@ __global__ void __launch_bounds__(kBlockX)
 nat_gather_k(Geo g, NativeParams np, const typename Store<ST>::T* __restrict__ src,
              typename Store<ST>::T* __restrict__ n_out, float* __restrict__ rho_f,
              float* __restrict__ u_f, const uint8_t* __restrict__ types) {
+    using R = typename Store<ST>::R;
     const int x = blockIdx.x * kBlockX + threadIdx.x;
     const int y = blockIdx.y, z = blockIdx.z;
     if (x >= g.nx) return;
@@ -210,26 +324,26 @@ nat_gather_k(Geo g, NativeParams np, const typename Store<ST>::T* __restrict__ s
                 u_f[node] = ub[0]; u_f[g.ks + node] = ub[1]; u_f[2 * g.ks + node] = ub[2];
             }
             if (n_out) {
+                // a solid node holds no populations: they read back as 0
 #pragma unroll
-                for (int k = 0; k < Q; ++k) Store<ST>::st(n_out, k * g.ks + node, ST == 0 ? 0.0f : -weight<Q>(k));
+                for (int k = 0; k < Q; ++k) Store<ST>::st(n_out, k * g.ks + node, ST == 1 ? -weight<Q>(k) : (R)0);
             }
             return;
         }
         near = (t & kNearSolid) != 0;
     }
     const Nbr nb(g, x, y, z);
-    float f[Q];
+    R f[Q];
     gather_node<Q, ST, MASK>(src, g, types, nb, node, near, f);
     if (n_out) {
 #pragma unroll
         for (int k = 0; k < Q; ++k) Store<ST>::st(n_out, k * g.ks + node, f[k]);
     }
     if (rho_f) {
-        float rho, ux, uy, uz;
-        if (ST == 0) node_moments<Q>(f, rho, ux, uy, uz);
-        else { float drho; node_moments_dev<Q>(f, drho, rho, ux, uy, uz); }
-        rho_f[node] = rho;
-        u_f[node] = ux; u_f[g.ks + node] = uy; u_f[2 * g.ks + node] = uz;
+        R rho, ux, uy, uz;
+        moments_any<Q, ST>(f, rho, ux, uy, uz);
+        rho_f[node] = (float)rho;
+        u_f[node] = (float)ux; u_f[g.ks + node] = (float)uy; u_f[2 * g.ks + node] = (float)uz;
     }
 }
 
@@ -307,13 +421,24 @@ int launch_raw(const Geo& g, const CollideParams& cp, const NativeParams& np, co
     return (int)cudaGetLastError();
 }
 
-// storage x mask x arith expansion for one Q
+template <int Q, int ST, bool MASK>
+int launch_gather(const Geo& g, const NativeParams& np, const void* src, void* n_out, float* rho, float* u,
+                  const uint8_t* types, cudaStream_t st) {
+    using T = typename Store<ST>::T;
+    nat_gather_k<Q, ST, MASK><<<cell_grid(g), kBlockX, 0, st>>>(g, np, (const T*)src, (T*)n_out, rho, u, types);
+    return (int)cudaGetLastError();
+}
+
+// storage x mask x arith expansion for one Q (FP16 and FP64 have one arithmetic each)
 template <int Q>
 int fused_q(int storage, int arith, bool m, const Geo& g, const CollideParams& cp, const NativeParams& np,
             const void* src, void* dst, const uint8_t* types, cudaStream_t st) {
     if (storage == 1)
         return m ? launch_fused<Q, 1, true, kArithFP32>(g, cp, np, src, dst, types, st)
                  : launch_fused<Q, 1, false, kArithFP32>(g, cp, np, src, dst, types, st);
+    if (storage == 2)
+        return m ? launch_fused<Q, 2, true, kArithFP32>(g, cp, np, src, dst, types, st)
+                 : launch_fused<Q, 2, false, kArithFP32>(g, cp, np, src, dst, types, st);
     if (arith == kArithReference)
         return m ? launch_fused<Q, 0, true, kArithReference>(g, cp, np, src, dst, types, st)
                  : launch_fused<Q, 0, false, kArithReference>(g, cp, np, src, dst, types, st);
@@ -327,19 +452,14 @@ int raw_q(int storage, int arith, bool m, const Geo& g, const CollideParams& cp,
     if (storage == 1)
         return m ? launch_raw<Q, 1, true, kArithFP32>(g, cp, np, src, dst, rho, u, types, st)
                  : launch_raw<Q, 1, false, kArithFP32>(g, cp, np, src, dst, rho, u, types, st);
+    if (storage == 2)
+        return m ? launch_raw<Q, 2, true, kArithFP32>(g, cp, np, src, dst, rho, u, types, st)
+                 : launch_raw<Q, 2, false, kArithFP32>(g, cp, np, src, dst, rho, u, types, st);
     if (arith == kArithReference)
         return m ? launch_raw<Q, 0, true, kArithReference>(g, cp, np, src, dst, rho, u, types, st)
                  : launch_raw<Q, 0, false, kArithReference>(g, cp, np, src, dst, rho, u, types, st);
     return m ? launch_raw<Q, 0, true, kArithFP32>(g, cp, np, src, dst, rho, u, types, st)
              : launch_raw<Q, 0, false, kArithFP32>(g, cp, np, src, dst, rho, u, types, st);
-}
-
-template <int Q, int ST, bool MASK>
-int launch_gather(const Geo& g, const NativeParams& np, const void* src, void* n_out, float* rho, float* u,
-                  const uint8_t* types, cudaStream_t st) {
-    using T = typename Store<ST>::T;
-    nat_gather_k<Q, ST, MASK><<<cell_grid(g), kBlockX, 0, st>>>(g, np, (const T*)src, (T*)n_out, rho, u, types);
-    return (int)cudaGetLastError();
 }
 
 template <int Q>
@@ -348,6 +468,9 @@ int gather_q(int storage, bool m, const Geo& g, const NativeParams& np, const vo
     if (storage == 1)
         return m ? launch_gather<Q, 1, true>(g, np, src, n_out, rho, u, types, st)
                  : launch_gather<Q, 1, false>(g, np, src, n_out, rho, u, types, st);
+    if (storage == 2)
+        return m ? launch_gather<Q, 2, true>(g, np, src, n_out, rho, u, types, st)
+                 : launch_gather<Q, 2, false>(g, np, src, n_out, rho, u, types, st);
     return m ? launch_gather<Q, 0, true>(g, np, src, n_out, rho, u, types, st)
              : launch_gather<Q, 0, false>(g, np, src, n_out, rho, u, types, st);
 }

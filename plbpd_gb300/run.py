@@ -5,10 +5,12 @@
 Workloads
   periodic  NATIVE semantics, every face periodic (the fused pull kernel
             without a node-type mask)
-  duct      NATIVE semantics, periodic x, no-slip walls on y and z, body force
-  channel   REFERENCE semantics, D2Q9-style channel: periodic x, walls up/down
-            (plbpd's own operator sequence, bit-exact)
-Used for quick measurements and for small profiler captures.
+  duct      NATIVE semantics, periodic x, no-slip walls on y and z, body force;
+            --spheres adds the seeded random-sphere obstacles (15% solid)
+  channel   REFERENCE semantics, periodic x, walls up/down (plbpd's own
+            operator sequence, bit-exact with the reference)
+--nx/--ny/--nz override --n per axis.  Used for quick measurements and for
+small profiler captures.
 """
 from __future__ import annotations
 
@@ -19,28 +21,41 @@ import time
 from . import capi
 
 
-def params_for(workload: str, model: str, n: int, storage: str, arith: str):
-    nx = ny = nz = n
-    if model == "D2Q9":
+def nu_for_tau(tau: float) -> float:
+    import numpy as np
+    target = np.float32(tau)
+    nu = np.float32((tau - 0.5) / 3.0)
+    for _ in range(64):
+        t = np.float32(np.float32(3.0) * nu) + np.float32(0.5)
+        if t == target:
+            break
+        nu = np.nextafter(nu, np.float32(np.inf) if t < target else np.float32(-np.inf))
+    return float(nu)
+
+
+def params_for(a):
+    nx, ny, nz = a.nx or a.n, a.ny or a.n, a.nz or a.n
+    if a.model == "D2Q9":
         ny = 1
-    st = capi.STORAGE_FP16_DEV if storage == "fp16" else capi.STORAGE_FP32
-    ar = capi.ARITH_REFERENCE if arith == "reference" else capi.ARITH_FP32
-    if workload == "periodic":
+    st = capi.STORAGE_FP16_DEV if a.storage == "fp16" else capi.STORAGE_FP32
+    ar = capi.ARITH_REFERENCE if a.arith == "reference" else capi.ARITH_FP32
+    nu = nu_for_tau(a.tau)
+    if a.workload == "periodic":
         faces = {f: "periodic" for f in capi.FACES}
-        return capi.make_params(model, nx, ny, nz, 0.0333333, face_type=faces, u0=(0.01, 0.0, 0.0),
+        return capi.make_params(a.model, nx, ny, nz, nu, face_type=faces, u0=(0.01, 0.0, 0.0),
                                 semantics=capi.SEMANTICS_NATIVE, arith=ar, storage=st)
-    if workload == "duct":
+    if a.workload == "duct":
         faces = {"east": "periodic", "west": "periodic", "north": "noslip", "south": "noslip", "up": "noslip",
                  "down": "noslip"}
         vel = {f: (0.0, 0.0, 0.0) for f in ("north", "south", "up", "down")}
-        return capi.make_params(model, nx, ny, nz, 0.0166667, force=(1e-6, 0.0, 0.0), face_type=faces, face_vel=vel,
+        return capi.make_params(a.model, nx, ny, nz, nu, force=(a.force, 0.0, 0.0), face_type=faces, face_vel=vel,
                                 semantics=capi.SEMANTICS_NATIVE, arith=ar, storage=st)
-    if workload == "channel":
+    if a.workload == "channel":
         faces = {"east": "periodic", "west": "periodic", "up": "noslip", "down": "noslip"}
         vel = {"up": (0.0, 0.0, 0.0), "down": (0.0, 0.0, 0.0)}
-        return capi.make_params(model, nx, ny, nz, 0.1, force=(1e-6, 0.0, 0.0), face_type=faces, face_vel=vel,
+        return capi.make_params(a.model, nx, ny, nz, nu, force=(a.force, 0.0, 0.0), face_type=faces, face_vel=vel,
                                 semantics=capi.SEMANTICS_REFERENCE, arith=ar)
-    raise SystemExit(f"unknown workload {workload}")
+    raise SystemExit(f"unknown workload {a.workload}")
 
 
 def main(argv=None):
@@ -48,22 +63,33 @@ def main(argv=None):
     ap.add_argument("--workload", default="periodic", choices=["periodic", "duct", "channel"])
     ap.add_argument("--model", default="D3Q19", choices=["D2Q9", "D3Q19", "D3Q27"])
     ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--nx", type=int, default=0)
+    ap.add_argument("--ny", type=int, default=0)
+    ap.add_argument("--nz", type=int, default=0)
+    ap.add_argument("--tau", type=float, default=0.6)
+    ap.add_argument("--force", type=float, default=1e-6)
+    ap.add_argument("--spheres", action="store_true")
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16"])
     ap.add_argument("--arith", default="fp32", choices=["fp32", "reference"])
     a = ap.parse_args(argv)
-    p = params_for(a.workload, a.model, a.n, a.storage, a.arith)
+    p = params_for(a)
     cells = int(p.nx) * int(p.ny) * int(p.nz)
     with capi.Solve(p) as s:
+        if a.spheres:
+            from .workloads import sphere_mask
+            s.set_mask(sphere_mask(int(p.nx), int(p.ny), int(p.nz)))
         s.initialize()
         s.step(a.warmup)
+        s.synchronize()
         t0 = time.perf_counter()
         s.step(a.steps)
         dt = time.perf_counter() - t0
-        print(json.dumps({"workload": a.workload, "model": a.model, "n": a.n, "storage": a.storage,
-                          "arith": a.arith, "steps": a.steps, "mlups": round(cells * a.steps / dt / 1e6, 1),
-                          "mass": s.conservation()[0]}))
+        print(json.dumps({"workload": a.workload, "model": a.model, "dims": [int(p.nx), int(p.ny), int(p.nz)],
+                          "storage": a.storage, "arith": a.arith, "spheres": a.spheres, "steps": a.steps,
+                          "seconds": round(dt, 4), "mlups": round(cells * a.steps / dt / 1e6, 1),
+                          "mass": s.conservation()[0], "device_bytes": s.device_bytes()}))
 
 
 if __name__ == "__main__":

@@ -71,3 +71,19 @@ SOURCEMAP_CASES = {
 CHANNEL = dict(model="D2Q9", nx=128, ny=1, nz=64, nu=0.1, rho0=1.0, u0=(0.0, 0.0, 0.0), force=(2.08e-6, 0.0, 0.0),
                rho_solid=1.0, face_type={"east": "periodic", "west": "periodic", "up": "noslip", "down": "noslip"},
                face_vel={"up": (0.0, 0.0, 0.0), "down": (0.0, 0.0, 0.0)})
+
+# plbpd's four Flow presets (src/Flow.cpp:20-106) with their step counts, as
+# explicit configurations for the reference harness.
+_XY = {"east": "periodic", "west": "periodic", "north": "periodic", "south": "periodic", "up": "noslip",
+       "down": "noslip"}
+_X = {"east": "periodic", "west": "periodic", "up": "noslip", "down": "noslip"}
+PRESETS = {
+    "Couette2D": (dict(model="D2Q9", nx=100, ny=1, nz=25, nu=0.5, rho0=1.0, u0=(0, 0, 0), force=(0, 0, 0),
+                       rho_solid=1.0, face_type=_X, face_vel={"up": (0.5, 0, 0), "down": (0, 0, 0)}), 20000),
+    "Couette3D": (dict(model="D3Q19", nx=200, ny=50, nz=50, nu=0.5, rho0=1.0, u0=(0, 0, 0), force=(0, 0, 0),
+                       rho_solid=1.0, face_type=_XY, face_vel={"up": (0.5, 0, 0), "down": (0, 0, 0)}), 200),
+    "Poiseuille2D": (dict(model="D2Q9", nx=256, ny=1, nz=48, nu=0.1, rho0=1.0, u0=(0, 0, 0), force=(1e-5, 0, 0),
+                          rho_solid=1.0, face_type=_X, face_vel={"up": (0, 0, 0), "down": (0, 0, 0)}), 5000),
+    "Poiseuille3D": (dict(model="D3Q19", nx=256, ny=256, nz=48, nu=0.1, rho0=1.0, u0=(0, 0, 0), force=(1e-5, 0, 0),
+                          rho_solid=1.0, face_type=_XY, face_vel={"up": (0, 0, 0), "down": (0, 0, 0)}), 10),
+}

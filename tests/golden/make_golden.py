@@ -13,7 +13,8 @@ Outputs
   * ``golden.json``  the known answers of the reference's unit tests
     (src/utest/TestEqlbDist.cpp:22-26, TestField.cpp:106-107, TestLBModel.cpp)
     as recomputed by the reference, plus SHA-256 digests of the reference's
-    final state on the 128x64 D2Q9 channel after 10,000 steps.
+    final state on the 128x64 D2Q9 channel after 10,000 steps and on the four
+    Flow presets (src/Flow.cpp:20-106) after their full step counts.
   * ``ref_sourcemap_<case>.npz``  the integer-encoded source map: n holds
     idx+1 and ntmp -(idx+1), wall velocities are zero, and one push, no-slip
     and periodic copy run; each output slot shows which slot it came from.
@@ -32,7 +33,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import pyoracle as po  # noqa: E402
 
-from cases import CASES, SOURCEMAP_CASES, CHANNEL  # noqa: E402
+from cases import CASES, CHANNEL, PRESETS, SOURCEMAP_CASES  # noqa: E402
 
 
 def fields(sim):
@@ -117,6 +118,13 @@ def main():
     sim.step(10000)
     g["channel_10000"] = {k: digest(v) for k, v in fields(sim).items()}
     g["channel_10000"]["u_max"] = float(sim.get(po.U)[1:-1, 1, 1:-1, 0].max())
+    # plbpd's Flow presets, full step counts, by the reference's own march
+    for name, (cfg, steps) in PRESETS.items():
+        sim = po.RefSim(**cfg, variant="avx2")
+        sim.initialize()
+        sim.step(steps)
+        g[f"preset_{name}"] = {k: digest(v) for k, v in fields(sim).items()}
+        g[f"preset_{name}"]["steps"] = steps
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(g, f, indent=1, sort_keys=True)
 

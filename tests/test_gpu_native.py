@@ -85,19 +85,24 @@ def p_face_solid(p):
     return solid
 
 
-@pytest.mark.parametrize("arith", ["fp32", "reference"])
+@pytest.mark.parametrize("arith", ["fp32", "reference", "fp16", "fp64"])
 @pytest.mark.parametrize("case", sorted(NATIVE_CASES))
 def test_native_matches_oracle(case, arith):
+    """FP32 storage with either arithmetic, FP16 deviation storage and FP64
+    storage, each bit-exact against the oracle's matching mode."""
     from plbpd_gb300 import capi
     cfg = NATIVE_CASES[case]
     mask = mask_for(case, cfg)
-    p = po.Port(**cfg, mode=po.MODE_NATIVE, arith=po.ARITH_FP32 if arith == "fp32" else po.ARITH_AVX2, mask=mask)
+    port_kw = {"fp32": dict(arith=po.ARITH_FP32), "reference": dict(arith=po.ARITH_AVX2),
+               "fp16": dict(arith=po.ARITH_FP16DEV), "fp64": dict(precision=1)}[arith]
+    gpu_kw = {"fp32": dict(arith=capi.ARITH_FP32), "reference": dict(arith=capi.ARITH_REFERENCE),
+              "fp16": dict(storage=capi.STORAGE_FP16_DEV), "fp64": dict(storage=capi.STORAGE_FP64)}[arith]
+    p = po.Port(**cfg, mode=po.MODE_NATIVE, mask=mask, **port_kw)
     p._cfg = cfg
     p.initialize()
     n, rho, u = perturbed_start(p, 11)
     p.set(po.N, n); p.set(po.RHO, rho); p.set(po.U, u)
-    with capi.Solve.create(**cfg, semantics=capi.SEMANTICS_NATIVE,
-                           arith=capi.ARITH_FP32 if arith == "fp32" else capi.ARITH_REFERENCE) as s:
+    with capi.Solve.create(**cfg, semantics=capi.SEMANTICS_NATIVE, **gpu_kw) as s:
         if mask is not None:
             s.set_mask(mask)
         s.initialize()
