@@ -169,6 +169,63 @@ int plb_synchronize(plb_solve* s);
  * work after plb_step_async. */
 void* plb_stream_handle(plb_solve* s);
 
+/* ---- batches of solves --------------------------------------------------------
+ * A batch advances many NATIVE solves of one lattice, storage and device
+ * together: every time step is one launch of a persistent-grid kernel whose
+ * resident blocks walk a list of 128-node tiles across all member domains,
+ * and the step loop replays as a captured CUDA graph.  Each domain keeps its
+ * own extents, tau, force, walls and mask, and its result is bit-identical
+ * to advancing it alone.  The batch does not own its solves; their own entry
+ * points (initialize, set/get field, set mask, conservation) still apply
+ * between batch calls.  No counterpart in plbpd, which runs one problem per
+ * process. */
+typedef struct plb_batch plb_batch;
+int plb_batch_create(int32_t n, plb_solve* const* solves, plb_batch** out);
+int plb_batch_step(plb_batch* b, int64_t nsteps);
+int plb_batch_step_async(plb_batch* b, int64_t nsteps);
+int plb_batch_synchronize(plb_batch* b);
+int plb_batch_destroy(plb_batch* b);
+/* Cells of all member domains. */
+int64_t plb_batch_cells(const plb_batch* b);
+
+/* ---- serving ------------------------------------------------------------------
+ * A server runs a scheduler thread that takes solve requests as they arrive,
+ * admits them while their device bytes fit a budget, keeps each admitted
+ * solve resident in HBM, and advances all running solves of one lattice /
+ * storage / arithmetic class together as one batch (classes on their own
+ * streams, so their kernels overlap), a tick of steps at a time.  A finished
+ * solve's rho and u are copied out and its memory is freed at once, so
+ * queued requests start as soon as room frees up.  Results are identical to
+ * running each request alone.  No counterpart in plbpd. */
+typedef struct plb_server plb_server;
+typedef struct plb_request {
+    plb_params params;      /* NATIVE semantics                                  */
+    const uint8_t* mask;    /* nz*ny*nx obstacle bytes or NULL; copied on submit */
+    int64_t steps;          /* time steps to run                                 */
+} plb_request;
+#define PLB_REQ_QUEUED 0
+#define PLB_REQ_RUNNING 1
+#define PLB_REQ_DONE 2
+#define PLB_REQ_FAILED 3
+/* Device bytes a solve with these parameters holds while it runs. */
+int64_t plb_solve_bytes(const plb_params* params);
+/* tick_steps: most steps a class advances between admission checks. */
+int plb_server_start(int32_t device, int64_t budget_bytes, int32_t tick_steps, plb_server** out);
+/* Thread-safe; the request (and its mask) is copied.  *id names it later. */
+int plb_server_submit(plb_server* srv, const plb_request* req, int64_t* id);
+int plb_server_status(plb_server* srv, int64_t id, int32_t* state);
+/* Blocks until the request is done or failed, or timeout_s passes (PLB_ETIMEOUT). */
+int plb_server_wait(plb_server* srv, int64_t id, double timeout_s);
+/* Copies a finished request's rho (plb_field_len RHO floats) and u (U floats)
+ * in plbpd's layout, either may be NULL, and times3 = seconds since the
+ * server started at submit, admission and completion; then forgets the
+ * request.  PLB_ESTATE while it is not done. */
+int plb_server_result(plb_server* srv, int64_t id, float* rho, float* u, double* times3);
+/* Bytes of the budget in use now, and the most in use at any time. */
+int plb_server_memory(plb_server* srv, int64_t* in_use, int64_t* peak);
+/* Finishes nothing further: pending and running requests are dropped. */
+int plb_server_stop(plb_server* srv);
+
 /* ---- the unfused plbpd operators (REFERENCE semantics) ---------------------
  * Each runs one operator of plbpd's loop on the device state, with plbpd's
  * semantics, so the plbpd classes can be driven operator by operator.     */

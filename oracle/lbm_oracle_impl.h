@@ -39,14 +39,16 @@ static void FN(collide_node)(const orc_sim* s, R* nl, R rho, const R* ul, R drho
         cu[k] = (float)s->c[k][0] * uu[0] + (float)s->c[k][1] * uu[1] +
                 (float)s->c[k][2] * uu[2];
     if (s->arith == ORC_ARITH_FP16DEV) {
-        /* deviation form: nl holds d = f - w */
+        /* deviation form: nl holds d = f - w;
+         * X = 3cu + 4.5cu^2 - 1.5usq, d' = (1-omega) d + w (omega rho X + omega drho) */
         const float kusq16 = -1.5f * usq;
+        const float orho = omega * rho;
+        const float odrho = omega * drho;
         for (int k = 0; k < q; ++k) {
-            float t = fmaf(4.5f, cu[k] * cu[k], kusq16);
-            t = fmaf(3.0f, cu[k], t);
-            float e = fmaf(rho, t, drho);
-            e = s->w[k] * e;
-            nl[k] = fmaf(1.0f - omega, nl[k], omega * e);
+            const float A = s->w[k] * orho;
+            const float B = s->w[k] * odrho;
+            const float X = fmaf(cu[k], fmaf(4.5f, cu[k], 3.0f), kusq16);
+            nl[k] = fmaf(1.0f - omega, nl[k], fmaf(A, X, B));
         }
         return;
     }

@@ -69,6 +69,20 @@ _SIGS = [
     ("plb_conservation", C.c_int, [C.c_void_p, C.c_void_p]),
     ("plb_conservation_static", C.c_int, [C.c_int32, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
                                           C.c_void_p]),
+    ("plb_batch_create", C.c_int, [C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("plb_batch_step", C.c_int, [C.c_void_p, C.c_int64]),
+    ("plb_batch_step_async", C.c_int, [C.c_void_p, C.c_int64]),
+    ("plb_batch_synchronize", C.c_int, [C.c_void_p]),
+    ("plb_batch_destroy", C.c_int, [C.c_void_p]),
+    ("plb_batch_cells", C.c_int64, [C.c_void_p]),
+    ("plb_solve_bytes", C.c_int64, [C.POINTER(Params)]),
+    ("plb_server_start", C.c_int, [C.c_int32, C.c_int64, C.c_int32, C.POINTER(C.c_void_p)]),
+    ("plb_server_submit", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]),
+    ("plb_server_status", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int32)]),
+    ("plb_server_wait", C.c_int, [C.c_void_p, C.c_int64, C.c_double]),
+    ("plb_server_result", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("plb_server_memory", C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    ("plb_server_stop", C.c_int, [C.c_void_p]),
     ("plb_host_alloc", C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
     ("plb_host_free", C.c_int, [C.c_void_p]),
     ("plb_device_bytes", C.c_int64, [C.c_void_p]),
@@ -252,3 +266,37 @@ class PinnedBuffer:
             self.free()
         except Exception:
             pass
+
+
+class Batch:
+    """Many NATIVE solves advanced together (plb_batch); the solves stay
+    usable on their own between batch calls."""
+
+    def __init__(self, solves):
+        self.solves = list(solves)
+        arr = (C.c_void_p * len(self.solves))(*[s.h.value for s in self.solves])
+        h = C.c_void_p()
+        check(lib().plb_batch_create(len(self.solves), C.cast(arr, C.c_void_p), C.byref(h)))
+        self.h = h
+
+    def step(self, n: int = 1) -> None: check(lib().plb_batch_step(self.h, int(n)))
+    def step_async(self, n: int = 1) -> None: check(lib().plb_batch_step_async(self.h, int(n)))
+    def synchronize(self) -> None: check(lib().plb_batch_synchronize(self.h))
+    def cells(self) -> int: return int(lib().plb_batch_cells(self.h))
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().plb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -5,6 +5,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "../../include/plb.h"
 #include "engine.h"
@@ -114,6 +115,7 @@ struct plb_solve {
     float* consts = nullptr;     // 2q floats: equilibrium(rho0, u0), weights
     uint8_t* types = nullptr;    // NATIVE node types
     uint8_t* types_tmp = nullptr;
+    uint32_t* links = nullptr;   // NATIVE solid-link masks
     uint8_t* mask_dev = nullptr;
     bool has_mask = false;       // NATIVE: walls or obstacles exist
     float* staging = nullptr;    // plbpd-layout transfer buffer
@@ -162,7 +164,7 @@ void release(plb_solve* s) {
     if (!s) return;
     drop_graphs(s);
     for (void* ptr : {s->f[0], s->f[1], (void*)s->rho, (void*)s->u, (void*)s->consts, (void*)s->types,
-                      (void*)s->types_tmp, (void*)s->mask_dev, (void*)s->staging, (void*)s->partials,
+                      (void*)s->types_tmp, (void*)s->links, (void*)s->mask_dev, (void*)s->staging, (void*)s->partials,
                       (void*)s->out4})
         if (ptr) cudaFree(ptr);
     if (s->out4_host) cudaFreeHost(s->out4_host);
@@ -202,9 +204,14 @@ void set_face_params(plb_solve* s, float rho_solid, const int32_t* face_type, co
     s->fp.cs2inv = cs2inv;
     s->fp.ew_periodic = face_type[0] == PLB_FACE_PERIODIC && face_type[1] == PLB_FACE_PERIODIC;
     s->fp.ns_periodic = face_type[2] == PLB_FACE_PERIODIC && face_type[3] == PLB_FACE_PERIODIC;
+    const uint32_t* links = s->np.links;
     std::memset(&s->np, 0, sizeof(s->np));
+    s->np.links = links;
     for (int f = 0; f < 6; ++f)
-        for (int i = 0; i < 3; ++i) s->np.vel[f][i] = s->fp.vel[f][i];
+        for (int i = 0; i < 3; ++i) {
+            s->np.vel[f][i] = s->fp.vel[f][i];
+            if (face_type[f] == PLB_FACE_NOSLIP && s->fp.vel[f][i] != 0.0f) s->np.moving = 1;
+        }
     s->np.rho_solid = rho_solid;
     s->np.cs2inv = cs2inv;
     const long long ext[3] = {s->p.nx, s->p.ny, s->p.nz};
@@ -263,9 +270,10 @@ int validate(const plb_params* p) {
     return PLB_OK;
 }
 
-int ensure_staging(plb_solve* s) {
+// Transfer buffer for one field of v components (grown on demand).
+int ensure_staging(plb_solve* s, int v) {
     const size_t cells = (size_t)(s->p.nx + 2) * (s->p.ny + 2) * (s->p.nz + 2);
-    const size_t need = cells * (size_t)(s->q > 3 ? s->q : 3);
+    const size_t need = cells * (size_t)v;
     if (s->staging && s->staging_len >= need) return PLB_OK;
     if (s->staging) { cudaFree(s->staging); s->device_bytes -= (int64_t)(s->staging_len * sizeof(float)); s->staging = nullptr; }
     PLB_TRY(dalloc(s, (void**)&s->staging, need * sizeof(float)));
@@ -514,9 +522,12 @@ int plb_solve_create(const plb_params* params, plb_solve** out) {
         s->has_mask = s->fp.noslip_mask != 0;
         if ((rc = dalloc(s, (void**)&s->types, (size_t)g.ks)) != PLB_OK) return bail(rc);
         if ((rc = dalloc(s, (void**)&s->types_tmp, (size_t)g.ks)) != PLB_OK) return bail(rc);
+        if ((rc = dalloc(s, (void**)&s->links, (size_t)g.ks * sizeof(uint32_t))) != PLB_OK) return bail(rc);
+        s->np.links = s->links;
         if (cudaMemsetAsync(s->types, 0, (size_t)g.ks, s->stream) != cudaSuccess)
             return bail(fail(PLB_ECUDA, "cudaMemsetAsync(types)"));
-        const int e = nat_build_types(s->q, g, nullptr, s->fp.noslip_mask, s->types_tmp, s->types, s->stream);
+        const int e = nat_build_types(s->q, g, nullptr, s->fp.noslip_mask, s->types_tmp, s->types, s->links,
+                                      s->stream);
         if (e != 0) return bail(fail(PLB_ECUDA, "nat_build_types"));
         s->post = false;
     }
@@ -574,6 +585,7 @@ int plb_set_mask(plb_solve* s, const uint8_t* mask) {
     if (!s->mask_dev) PLB_TRY(dalloc(s, (void**)&s->mask_dev, cells));
     if (mask) PLB_CUDA(cudaMemcpyAsync(s->mask_dev, mask, cells, cudaMemcpyHostToDevice, s->stream));
     PLB_KERNEL(nat_build_types(s->q, s->g, mask ? s->mask_dev : nullptr, s->fp.noslip_mask, s->types_tmp, s->types,
+                               s->links,
                                s->stream));
     s->has_mask = mask != nullptr || s->fp.noslip_mask != 0;
     drop_graphs(s);
@@ -701,7 +713,7 @@ int plb_get_field(plb_solve* s, int32_t which, float* out) {
     } else if (which == PLB_FIELD_RHO || which == PLB_FIELD_U) {
         PLB_TRY(ref_materialize_fields(s));
     }
-    PLB_TRY(ensure_staging(s));
+    PLB_TRY(ensure_staging(s, (int)(len / ((size_t)(s->p.nx + 2) * (s->p.ny + 2) * (s->p.nz + 2)))));
     const float* wk = s->consts + s->q;
     if (which == PLB_FIELD_N || which == PLB_FIELD_NTMP) {
         const void* src = s->f[which == PLB_FIELD_N ? n_buf : 1 - s->cur];
@@ -724,8 +736,8 @@ int plb_set_field(plb_solve* s, int32_t which, const float* in) {
     } else {
         PLB_TRY(ref_materialize_fields(s));
     }
-    PLB_TRY(ensure_staging(s));
     const size_t len = plb_field_len(s, which);
+    PLB_TRY(ensure_staging(s, (int)(len / ((size_t)(s->p.nx + 2) * (s->p.ny + 2) * (s->p.nz + 2)))));
     PLB_CUDA(cudaMemcpyAsync(s->staging, in, len * sizeof(float), cudaMemcpyHostToDevice, s->stream));
     if (which == PLB_FIELD_N || which == PLB_FIELD_NTMP) {
         void* dst = s->f[which == PLB_FIELD_N ? s->cur : 1 - s->cur];
@@ -741,7 +753,16 @@ int plb_set_field(plb_solve* s, int32_t which, const float* in) {
 int plb_conservation(plb_solve* s, double* out4) {
     if (!s || !out4) return fail(PLB_EINVAL, "null argument");
     PLB_TRY(set_device(s));
-    PLB_KERNEL(util_conservation(s->q, s->storage, s->g, s->f[s->cur], s->native ? s->types : nullptr,
+    // the sums are of the current populations n_t; under NATIVE semantics the
+    // state may be P_{t-1}, whose bounce-back slots hold reversed directions,
+    // so n_t is gathered first (mass alone would not need it, momentum does)
+    int buf = s->cur;
+    if (s->native && s->post) {
+        PLB_KERNEL(nat_gather(s->q, s->storage, s->has_mask, s->g, s->np, s->f[s->cur], s->f[1 - s->cur], nullptr,
+                              nullptr, s->types, s->stream));
+        buf = 1 - s->cur;
+    }
+    PLB_KERNEL(util_conservation(s->q, s->storage, s->g, s->f[buf], s->native ? s->types : nullptr,
                                  s->fp.noslip_mask, s->partials, s->out4, s->stream));
     PLB_CUDA(cudaMemcpyAsync(s->out4_host, s->out4, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     PLB_TRY(sync(s));
@@ -761,5 +782,196 @@ int plb_host_free(void* p) {
 }
 
 int64_t plb_device_bytes(const plb_solve* s) { return s ? s->device_bytes : 0; }
+
+}  // extern "C"
+
+// ===========================================================================
+// batches
+struct plb_batch {
+    std::vector<plb_solve*> solves;
+    int q = 0, storage = 0, arith = 0, device = 0;
+    cudaStream_t stream = nullptr;
+    BatchDomain* d_doms = nullptr;
+    int4* d_tiles = nullptr;   // warp tasks (domain, y, z, x0)
+    int ntiles = 0;
+    int blocks = 0;
+    int64_t cells = 0;
+    bool moving = false;   // some member has a moving wall
+    int graph_steps = 64;
+    cudaGraphExec_t graph = nullptr;
+    std::vector<BatchDomain> h_doms;
+};
+
+namespace {
+
+void batch_release(plb_batch* b) {
+    if (!b) return;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->d_doms) cudaFree(b->d_doms);
+    if (b->d_tiles) cudaFree(b->d_tiles);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+// Brings every member to the POST state with one step where needed: members
+// in RAW take their first collision, members already in POST one fused step,
+// so all advance by exactly one step.  Returns the step count consumed.
+int batch_prepare(plb_batch* b, int64_t* consumed) {
+    bool any_raw = false;
+    for (plb_solve* s : b->solves) any_raw |= !s->post;
+    *consumed = 0;
+    if (!any_raw) return PLB_OK;
+    for (plb_solve* s : b->solves) {
+        if (!s->post) {
+            PLB_KERNEL(nat_collide_raw(s->q, s->storage, s->p.arith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
+                                       s->f[1 - s->cur], s->rho, s->u, s->types, b->stream));
+            s->post = true;
+        } else {
+            PLB_KERNEL(nat_fused_step(s->q, s->storage, s->p.arith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
+                                      s->f[1 - s->cur], s->types, b->stream));
+        }
+        s->cur = 1 - s->cur;
+    }
+    *consumed = 1;
+    return PLB_OK;
+}
+
+// Device table of the members, each with its buffers ordered so that
+// f[0] is the one holding the current state.
+int batch_upload_table(plb_batch* b) {
+    for (size_t i = 0; i < b->solves.size(); ++i) {
+        plb_solve* s = b->solves[i];
+        BatchDomain& d = b->h_doms[i];
+        d.g = s->g;
+        d.cp = s->cp;
+        d.np = s->np;
+        d.types = s->types;
+        d.f[0] = s->f[s->cur];
+        d.f[1] = s->f[1 - s->cur];
+    }
+    PLB_CUDA(cudaMemcpyAsync(b->d_doms, b->h_doms.data(), b->h_doms.size() * sizeof(BatchDomain),
+                             cudaMemcpyHostToDevice, b->stream));
+    return PLB_OK;
+}
+
+int batch_capture(plb_batch* b) {
+    cudaGraph_t graph = nullptr;
+    PLB_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = 0;
+    for (int i = 0; i < b->graph_steps && rc == 0; ++i)
+        rc = nat_batch_step(b->q, b->storage, b->arith, b->moving, b->d_doms, b->d_tiles, b->ntiles, i & 1,
+                            b->blocks, b->stream);
+    const cudaError_t ec = cudaStreamEndCapture(b->stream, &graph);
+    if (rc != 0) {
+        if (graph) cudaGraphDestroy(graph);
+        return fail(PLB_ECUDA, std::string("batch capture: ") + cudaGetErrorString((cudaError_t)rc));
+    }
+    if (ec != cudaSuccess) return fail(PLB_ECUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ec));
+    const cudaError_t ei = cudaGraphInstantiate(&b->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) return fail(PLB_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ei));
+    return PLB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int plb_batch_create(int32_t n, plb_solve* const* solves, plb_batch** out) {
+    if (!out || !solves || n < 1) return fail(PLB_EINVAL, "a batch needs at least one solve");
+    *out = nullptr;
+    const plb_solve* s0 = solves[0];
+    if (!s0) return fail(PLB_EINVAL, "null solve");
+    for (int i = 0; i < n; ++i) {
+        const plb_solve* s = solves[i];
+        if (!s) return fail(PLB_EINVAL, "null solve");
+        if (!s->native) return fail(PLB_EUNSUPPORTED, "batches need NATIVE semantics");
+        if (s->q != s0->q || s->storage != s0->storage || s->p.arith != s0->p.arith || s->p.device != s0->p.device)
+            return fail(PLB_EINVAL, "batch members must share lattice, storage, arithmetic and device");
+        if (s->storage == PLB_STORAGE_FP64) return fail(PLB_EUNSUPPORTED, "FP64 storage is not batched");
+        if ((long long)s->g.ys * s->g.ny * s->g.nz >= (1ll << 31))
+            return fail(PLB_EINVAL, "batch member too large for 32-bit tile indices");
+    }
+    plb_batch* b = new plb_batch();
+    b->solves.assign(solves, solves + n);
+    b->q = s0->q; b->storage = s0->storage; b->arith = s0->p.arith; b->device = s0->p.device;
+    b->graph_steps = graph_steps_default();
+    b->h_doms.resize(n);
+    if (cudaSetDevice(b->device) != cudaSuccess) { batch_release(b); return fail(PLB_ECUDA, "cudaSetDevice"); }
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        batch_release(b);
+        return fail(PLB_ECUDA, "cudaStreamCreate");
+    }
+    std::vector<int4> tiles;
+    for (int i = 0; i < n; ++i) {
+        const Geo& g = solves[i]->g;
+        for (int z = 0; z < g.nz; ++z)
+            for (int y = 0; y < g.ny; ++y)
+                for (int x0 = 0; x0 < g.nx; x0 += 32) tiles.push_back(make_int4(i, y, z, x0));
+        b->cells += g.cells();
+    }
+    b->ntiles = (int)tiles.size();
+    int dev_sms = 0;
+    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, b->device);
+    for (int i = 0; i < n; ++i) b->moving |= solves[i]->np.moving != 0;
+    const int per_sm = nat_batch_blocks_per_sm(b->q, b->storage, b->arith, b->moving);
+    b->blocks = (dev_sms > 0 ? dev_sms : 1) * (per_sm > 0 ? per_sm : 1);
+    if (cudaMalloc(&b->d_doms, n * sizeof(BatchDomain)) != cudaSuccess ||
+        cudaMalloc(&b->d_tiles, tiles.size() * sizeof(int4)) != cudaSuccess) {
+        batch_release(b);
+        return fail(PLB_ENOMEM, "batch tables");
+    }
+    if (cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess) {
+        batch_release(b);
+        return fail(PLB_ECUDA, "batch tile upload");
+    }
+    *out = b;
+    return PLB_OK;
+}
+
+int plb_batch_step_async(plb_batch* b, int64_t nsteps) {
+    if (!b) return fail(PLB_EINVAL, "batch is null");
+    if (nsteps < 0) return fail(PLB_EINVAL, "negative step count");
+    if (nsteps == 0) return PLB_OK;
+    PLB_CUDA(cudaSetDevice(b->device));
+    for (plb_solve* s : b->solves) PLB_TRY(sync(s));   // members' own work comes first
+    int64_t done = 0;
+    PLB_TRY(batch_prepare(b, &done));
+    PLB_TRY(batch_upload_table(b));
+    int64_t i = 0;
+    const int64_t todo = nsteps - done;
+    const int64_t G = b->graph_steps;
+    while (G > 0 && todo - i >= G) {
+        if (!b->graph) PLB_TRY(batch_capture(b));
+        PLB_CUDA(cudaGraphLaunch(b->graph, b->stream));
+        i += G;
+    }
+    for (; i < todo; ++i)
+        PLB_KERNEL(nat_batch_step(b->q, b->storage, b->arith, b->moving, b->d_doms, b->d_tiles, b->ntiles, (int)(i & 1),
+                                  b->blocks, b->stream));
+    if (todo & 1)
+        for (plb_solve* s : b->solves) s->cur = 1 - s->cur;
+    return PLB_OK;
+}
+
+int plb_batch_synchronize(plb_batch* b) {
+    if (!b) return fail(PLB_EINVAL, "batch is null");
+    PLB_CUDA(cudaStreamSynchronize(b->stream));
+    return PLB_OK;
+}
+
+int plb_batch_step(plb_batch* b, int64_t nsteps) {
+    PLB_TRY(plb_batch_step_async(b, nsteps));
+    return plb_batch_synchronize(b);
+}
+
+int plb_batch_destroy(plb_batch* b) {
+    if (!b) return PLB_OK;
+    cudaStreamSynchronize(b->stream);
+    batch_release(b);
+    return PLB_OK;
+}
+
+int64_t plb_batch_cells(const plb_batch* b) { return b ? b->cells : 0; }
 
 }  // extern "C"

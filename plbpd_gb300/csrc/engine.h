@@ -33,6 +33,8 @@ struct NativeParams {
     float vel[8][3];      // solid velocities by index (6 = obstacle = 0)
     float rho_solid;
     float cs2inv;
+    int moving;           // some wall velocity is nonzero
+    const uint32_t* links;  // per node: bit k set when x + c_k is solid
 };
 
 // ---- REFERENCE semantics (kernels_ref.cu) ----------------------------------
@@ -76,9 +78,29 @@ int nat_gather(int q, int storage, bool has_mask, const Geo& g, const NativePara
 int nat_reset_fields(const Geo& g, const NativeParams& np, const uint8_t* types, float* rho,
                      float* u, cudaStream_t st);
 // Node types from an obstacle mask (nz*ny*nx bytes, may be null) and the walls.
-// `scratch` has the size of `types`.
+// `scratch` has the size of `types`; `links` gets one word per node.
 int nat_build_types(int q, const Geo& g, const uint8_t* mask, int noslip_mask,
-                    uint8_t* scratch, uint8_t* types, cudaStream_t st);
+                    uint8_t* scratch, uint8_t* types, uint32_t* links, cudaStream_t st);
+
+// ---- batches of NATIVE domains (kernels_native.cu) --------------------------
+// One domain of a batch: its geometry, parameters and buffers.
+struct BatchDomain {
+    Geo g;
+    CollideParams cp;
+    NativeParams np;
+    const uint8_t* types;
+    void* f[2];
+};
+// A task is one warp's work: up to 32 nodes of one row of one domain,
+// (domain index, y, z, first x).
+// One launch advances every domain by one step, reading f[parity] and
+// writing f[parity ^ 1]; `blocks` resident blocks walk the task list.
+// `moving`: some member has a moving wall.
+int nat_batch_step(int q, int storage, int arith, bool moving, const BatchDomain* doms, const int4* tiles,
+                   int ntiles, int parity, int blocks, cudaStream_t st);
+// Resident blocks per SM of the batch kernel (for sizing the grid).
+int nat_batch_blocks_per_sm(int q, int storage, int arith, bool moving);
+constexpr int kBatchTile = 128;
 
 // ---- shared (kernels_util.cu) ----------------------------------------------
 // Every node of the box (halo included): rho0, u0, n = feq, ntmp = 0.

@@ -44,5 +44,28 @@ def sphere_mask(nx: int, ny: int, nz: int, solid_fraction: float = 0.15, rmin: f
     return mask
 
 
-def porous_mask(nx: int, ny: int, nz: int, porosity: float, seed: int, wrap=(True, False, False)) -> np.ndarray:
-    return sphere_mask(nx, ny, nz, solid_fraction=1.0 - porosity, rmin=1.0, rmax=3.0, seed=seed, wrap=wrap)
+def porous_mask(nx: int, ny: int, nz: int, porosity: float, seed: int) -> np.ndarray:
+    """Random obstacles of 2x2x2 cells: a coarse random field at half
+    resolution, solid where below 1 - porosity, upsampled."""
+    rng = np.random.default_rng(seed)
+    coarse = rng.random(((nz + 1) // 2, (ny + 1) // 2, (nx + 1) // 2)) < (1.0 - porosity)
+    fine = np.repeat(np.repeat(np.repeat(coarse, 2, axis=0), 2, axis=1), 2, axis=2)
+    return np.ascontiguousarray(fine[:nz, :ny, :nx]).astype(np.uint8)
+
+
+def batch_domains(count: int = 512, seed: int = 20261203, lmin: int = 16, lmax: int = 96):
+    """The batched workload: `count` cubes with edges log-uniform in
+    [lmin, lmax], tau uniform in [0.55, 1.2], porosity uniform in [0.7, 0.9],
+    periodic in x with resting walls elsewhere, body force for a channel
+    velocity of 0.02.  Yields (edge, tau, porosity, force_x, mask_seed)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        L = int(round(float(np.exp(rng.uniform(np.log(lmin), np.log(lmax))))))
+        tau = float(rng.uniform(0.55, 1.2))
+        por = float(rng.uniform(0.7, 0.9))
+        nu = (tau - 0.5) / 3.0
+        h = max(L - 2, 1)
+        force = 8.0 * nu * 0.02 / (h * h)
+        out.append((L, tau, por, force, seed + 1 + i))
+    return out

@@ -1,0 +1,79 @@
+"""Batches: many domains of different size, tau, force, walls and obstacles
+advanced together by the tile-list kernel give, bit for bit, what each domain
+gives advanced alone."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+DUCT = {"east": "periodic", "west": "periodic", "north": "noslip", "south": "noslip", "up": "noslip",
+        "down": "noslip"}
+REST = {f: (0.0, 0.0, 0.0) for f in ("north", "south", "up", "down")}
+
+
+def make_solves(capi, storage, seed=5, count=7, model="D3Q19"):
+    from plbpd_gb300.workloads import porous_mask
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        L = int(rng.integers(6, 30))
+        nx, ny, nz = L + int(rng.integers(0, 5)), L, L + int(rng.integers(0, 3))
+        if storage == capi.STORAGE_FP16_DEV:
+            nx += nx % 2
+        tau = float(rng.uniform(0.55, 1.2))
+        vel = dict(REST)
+        if i % 3 == 0:
+            vel["up"] = (0.02, 0.0, 0.0)   # a moving lid on some domains
+        s = capi.Solve.create(model, nx, ny, nz, (tau - 0.5) / 3.0, force=(float(rng.uniform(1e-6, 1e-4)), 0.0, 0.0),
+                              u0=(0.005, 0.0, 0.0), face_type=DUCT, face_vel=vel,
+                              semantics=capi.SEMANTICS_NATIVE, arith=capi.ARITH_FP32, storage=storage)
+        if i % 2 == 0:
+            s.set_mask(porous_mask(nx, ny, nz, float(rng.uniform(0.7, 0.9)), seed + i))
+        s.initialize()
+        out.append(s)
+    return out
+
+
+@pytest.mark.parametrize("storage_name", ["fp32", "fp16"])
+@pytest.mark.parametrize("model", ["D3Q19", "D3Q27"])
+def test_batch_equals_each_domain_alone(storage_name, model):
+    from plbpd_gb300 import capi
+    storage = capi.STORAGE_FP32 if storage_name == "fp32" else capi.STORAGE_FP16_DEV
+    mix = make_solves(capi, storage, model=model)
+    alone = make_solves(capi, storage, model=model)
+    with capi.Batch(mix) as b:
+        b.step(1)       # first collision from the initial state
+        b.step(140)     # graph chunks plus a tail
+        b.step(3)
+    for s in alone:
+        s.step(144)
+    for a, m in zip(alone, mix):
+        for w in (capi.FIELD_N, capi.FIELD_RHO, capi.FIELD_U):
+            ga, gm = a.get(w), m.get(w)
+            assert np.array_equal(ga.view(np.uint32), gm.view(np.uint32)), f"field {w} differs"
+        np.testing.assert_array_equal(a.conservation(), m.conservation())
+
+
+def test_batch_mixed_states():
+    """Members that were stepped on their own before joining stay in step."""
+    from plbpd_gb300 import capi
+    mix = make_solves(capi, capi.STORAGE_FP32, seed=9, count=4)
+    alone = make_solves(capi, capi.STORAGE_FP32, seed=9, count=4)
+    mix[1].step(3)
+    alone[1].step(3)
+    with capi.Batch(mix) as b:
+        b.step(10)
+    for s in alone:
+        s.step(10)
+    for a, m in zip(alone, mix):
+        assert np.array_equal(a.get(capi.FIELD_U).view(np.uint32), m.get(capi.FIELD_U).view(np.uint32))
+
+
+def test_batch_rejects_mixed_lattices():
+    from plbpd_gb300 import capi
+    a = capi.Solve.create("D3Q19", 8, 8, 8, 0.1, face_type={f: "periodic" for f in capi.FACES},
+                          semantics=capi.SEMANTICS_NATIVE)
+    b = capi.Solve.create("D3Q27", 8, 8, 8, 0.1, face_type={f: "periodic" for f in capi.FACES},
+                          semantics=capi.SEMANTICS_NATIVE)
+    with pytest.raises(capi.PlbError):
+        capi.Batch([a, b])
