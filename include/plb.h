@@ -80,6 +80,18 @@ extern "C" {
 #define PLB_STORAGE_FP16_DEV 1
 #define PLB_STORAGE_FP64 2
 
+/* Collision operator.  BGK is plbpd's CollisionSRT (src/CollisionSRT.cpp),
+ * body force as the velocity shift u + F tau/rho.  TRT is an extension
+ * through plbpd's Collision base (src/Collision.hpp:10-21), NATIVE semantics
+ * only, with PLB_ARITH_FP32 or FP16/FP64 storage: the even part of each pair
+ * of opposite directions relaxes with 1/tau, the odd part with 1/tau_m,
+ * tau_m = trt_magic/(tau - 1/2) + 1/2 (trt_magic 0 selects 3/16, which puts
+ * the half-way bounce-back wall exactly half way), and the force enters as a
+ * second-order source with v = u + F/(2 rho) in the equilibrium.  Exported u
+ * is sum(c_k f_k)/rho under both operators, as plbpd's CalcMoments reports it. */
+#define PLB_COLLISION_BGK 0
+#define PLB_COLLISION_TRT 1
+
 /* Field ids: plbpd's SimData members n, ntmp, rho, u (src/SimData.hpp:18-21). */
 #define PLB_FIELD_N 0
 #define PLB_FIELD_NTMP 1
@@ -108,6 +120,8 @@ typedef struct plb_params {
     int32_t arith;              /* PLB_ARITH_*                                      */
     int32_t storage;            /* PLB_STORAGE_*                                    */
     int32_t device;             /* CUDA device ordinal                              */
+    int32_t collision;          /* PLB_COLLISION_* (0: BGK)                         */
+    float trt_magic;            /* TRT: (tau - 1/2)(tau_m - 1/2); 0 selects 3/16    */
 } plb_params;
 
 /* ---- library ----------------------------------------------------------- */
@@ -187,16 +201,21 @@ int plb_batch_synchronize(plb_batch* b);
 int plb_batch_destroy(plb_batch* b);
 /* Cells of all member domains. */
 int64_t plb_batch_cells(const plb_batch* b);
+/* The batch's CUDA stream (a cudaStream_t). */
+void* plb_batch_stream_handle(plb_batch* b);
 
 /* ---- serving ------------------------------------------------------------------
  * A server runs a scheduler thread that takes solve requests as they arrive,
  * admits them while their device bytes fit a budget, keeps each admitted
- * solve resident in HBM, and advances all running solves of one lattice /
- * storage / arithmetic class together as one batch (classes on their own
- * streams, so their kernels overlap), a tick of steps at a time.  A finished
- * solve's rho and u are copied out and its memory is freed at once, so
- * queued requests start as soon as room frees up.  Results are identical to
- * running each request alone.  No counterpart in plbpd. */
+ * solve resident in HBM, and advances the running solves a tick of steps
+ * at a time: small solves of one lattice / storage / arithmetic class
+ * together as one batch, large ones (PLB_SERVER_SOLO_CELLS cells or more,
+ * default 2^19) alone with their own kernels.  Every batch and large solve
+ * runs on its own stream, so their kernels overlap, and the scheduler
+ * restarts each one as soon as its own tick ends.  A finished solve's rho
+ * and u are copied out and its memory is freed at once, so queued requests
+ * start as soon as room frees up.  Results are identical to running each
+ * request alone.  No counterpart in plbpd. */
 typedef struct plb_server plb_server;
 typedef struct plb_request {
     plb_params params;      /* NATIVE semantics                                  */

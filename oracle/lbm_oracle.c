@@ -18,11 +18,17 @@ struct orc_sim {
     long nx, ny, nz;      /* interior extents                        */
     long X, Y, Z;         /* extents with the halo: n + 2             */
     int32_t c[27][3];
-    float w[27];
+    float w[27];          /* plbpd's weights: double literals rounded to float */
+    double wd[27];        /* the exact weights in double, for precision 1:
+                             the float ones sum to 1 + O(1e-8), which a double
+                             run would add to the mass every collision */
     uint32_t rev[27];
     float cs2, cs2inv;
     float nu, rho0, u0[3], force[3], rho_solid;
     float tau, omega;
+    int trt;              /* NATIVE: two-relaxation-time collision       */
+    float omega_m;        /* TRT: odd-moment rate, float arithmetic      */
+    double omega_m_d;     /* TRT: odd-moment rate, double arithmetic     */
     int face_type[6], face_has_vel[6];
     float face_vel[6][3];
     int mode, arith, precision;
@@ -50,6 +56,13 @@ static const int32_t kD3Q27[27][3] = {
     {1, 1, 1}, {-1, -1, -1}, {1, 1, -1}, {-1, -1, 1}, {1, -1, 1}, {-1, 1, -1},
     {-1, 1, 1}, {1, -1, -1}};
 
+/* Weight of a velocity with |c|^2 = sp, as the reference's double literal. */
+static double weight_exact(int q, int sp) {
+    if (q == 9) return sp == 0 ? 4. / 9. : (sp == 1 ? 1. / 9. : 1. / 36.);
+    if (q == 19) return sp == 0 ? 1. / 3. : (sp == 1 ? 1. / 18. : 1. / 36.);
+    return sp == 0 ? 8. / 27. : (sp == 1 ? 2. / 27. : (sp == 2 ? 1. / 54. : 1. / 216.));
+}
+
 int orc_model_tables(int q, int32_t* c, float* w, uint32_t* rev, float* cs2) {
     const int32_t(*cv)[3];
     if (q == 9) cv = kD2Q9;
@@ -58,12 +71,7 @@ int orc_model_tables(int q, int32_t* c, float* w, uint32_t* rev, float* cs2) {
     else return 0;
     for (int k = 0; k < q; ++k) {
         for (int i = 0; i < 3; ++i) c[3 * k + i] = cv[k][i];
-        double wd;
-        const int s = abs(cv[k][0]) + abs(cv[k][1]) + abs(cv[k][2]);
-        if (q == 9) wd = s == 0 ? 4. / 9. : (s == 1 ? 1. / 9. : 1. / 36.);
-        else if (q == 19) wd = s == 0 ? 1. / 3. : (s == 1 ? 1. / 18. : 1. / 36.);
-        else wd = s == 0 ? 8. / 27. : (s == 1 ? 2. / 27. : (s == 2 ? 1. / 54. : 1. / 216.));
-        w[k] = (float)wd;
+        w[k] = (float)weight_exact(q, abs(cv[k][0]) + abs(cv[k][1]) + abs(cv[k][2]));
         /* every table lists each velocity directly before or after its opposite */
         rev[k] = k == 0 ? 0u : (uint32_t)(k % 2 == 1 ? k + 1 : k - 1);
     }
@@ -200,8 +208,10 @@ orc_sim* orc_create(int q, long nx, long ny, long nz, float nu, float rho0,
     if (!s) return NULL;
     int32_t c[27 * 3];
     if (!orc_model_tables(q, c, s->w, s->rev, &s->cs2)) { free(s); return NULL; }
-    for (int k = 0; k < q; ++k)
+    for (int k = 0; k < q; ++k) {
         for (int i = 0; i < 3; ++i) s->c[k][i] = c[3 * k + i];
+        s->wd[k] = weight_exact(q, abs(c[3 * k]) + abs(c[3 * k + 1]) + abs(c[3 * k + 2]));
+    }
     s->q = q;
     s->nx = nx; s->ny = ny; s->nz = nz;
     s->X = nx + 2; s->Y = ny + 2; s->Z = nz + 2;
@@ -257,6 +267,17 @@ void orc_destroy(orc_sim* s) {
     free(s->n); free(s->ntmp); free(s->rho); free(s->u);
     free(s->solid); free(s->solid_vel); free(s->drho);
     free(s);
+}
+
+int orc_set_trt(orc_sim* s, float magic) {
+    if (s->mode != ORC_MODE_NATIVE || !(s->tau > 0.5f)) return -1;
+    if (s->precision == 0 && s->arith != ORC_ARITH_FP32 && s->arith != ORC_ARITH_FP16DEV) return -1;
+    const double lam = magic > 0.0f ? (double)magic : 3.0 / 16.0;
+    const double tau_m = lam / ((double)s->tau - 0.5) + 0.5;
+    s->trt = 1;
+    s->omega_m_d = 1.0 / tau_m;
+    s->omega_m = (float)s->omega_m_d;
+    return 0;
 }
 
 int orc_set_mask(orc_sim* s, const uint8_t* mask) {

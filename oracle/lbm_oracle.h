@@ -63,7 +63,10 @@ int orc_model_tables(int q, int32_t* c, float* w, uint32_t* rev, float* cs2);
 void orc_eqlb(int q, float rho, const float* u, float* out);
 
 /* face order: east, west, north, south, up, down (src/Boundary.cpp:17-18).
- * precision: 0 = float, 1 = double.  Returns NULL on invalid input. */
+ * precision: 0 = float, 1 = double.  The double instantiation uses the exact
+ * weights (4/9, 1/9, ... in double, not plbpd's float ones, whose sum 1 +
+ * O(1e-8) would add mass at every collision): it is the accuracy reference
+ * reduced-precision runs are measured against.  Returns NULL on invalid input. */
 orc_sim* orc_create(int q, long nx, long ny, long nz, float nu, float rho0,
                     const float* u0, const float* force, float rho_solid,
                     const int* face_type, const int* face_has_vel,
@@ -71,6 +74,21 @@ orc_sim* orc_create(int q, long nx, long ny, long nz, float nu, float rho0,
 void orc_destroy(orc_sim* s);
 void orc_set_threads(int n);
 int orc_max_threads(void);
+
+/* Two-relaxation-time collision for ORC_MODE_NATIVE (float arithmetic
+ * ORC_ARITH_FP32 or ORC_ARITH_FP16DEV, or double precision).  The even part
+ * of each pair (k, r = rev k) relaxes with omega = 1/tau, the odd part with
+ * omega_m = 1/tau_m, tau_m = magic/(tau - 1/2) + 1/2 (magic 0 selects 3/16),
+ * and the body force enters as a second-order source (no velocity shift):
+ *   v = u + F/(2 rho),  f+ = (f_k + f_r)/2,  f- = (f_k - f_r)/2,
+ *   e+ = w rho (1 + 4.5(c.v)^2 - 1.5v^2),  e- = 3 w rho c.v,
+ *   S+ = (1 - omega/2) w (9 (c.v)(c.F) - 3 v.F),  S- = (1 - omega_m/2) 3 w c.F,
+ *   f_k' = f_k - omega (f+ - e+) - omega_m (f- - e-) + S+ + S-,
+ *   f_r' = f_r - omega (f+ - e+) + omega_m (f- - e-) + S+ - S-.
+ * With magic 3/16 and half-way bounce-back, plane Poiseuille flow is exact.
+ * Returns 0, or -1 when the mode, arithmetic or tau (must exceed 1/2) does
+ * not allow it. */
+int orc_set_trt(orc_sim* s, float magic);
 
 /* Obstacle mask for ORC_MODE_NATIVE: nz*ny*nx bytes (x fastest), nonzero = solid. */
 int orc_set_mask(orc_sim* s, const uint8_t* mask);

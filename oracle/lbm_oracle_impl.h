@@ -21,9 +21,41 @@ static void FN(collide_node)(const orc_sim* s, R* nl, R rho, const R* ul, R drho
     double uu[3];
     for (int i = 0; i < 3; ++i) uu[i] = ul[i] + (double)s->force[i] * trho;
     const double usq = uu[0] * uu[0] + uu[1] * uu[1] + uu[2] * uu[2];
+    if (s->trt) {
+        /* TRT with a second-order force source; pairs (k, k + 1), k odd
+         * (every table lists a velocity next to its opposite) */
+        const double omm = s->omega_m_d;
+        const double gp = 1.0 - 0.5 * omega, gm = 1.0 - 0.5 * omm;
+        const double hr = 0.5 / rho;
+        double v[3], F[3];
+        for (int i = 0; i < 3; ++i) { F[i] = (double)s->force[i]; v[i] = ul[i] + F[i] * hr; }
+        const double vsq = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+        const double uF = v[0] * F[0] + v[1] * F[1] + v[2] * F[2];
+        const double k15 = 1.5 * vsq, m3uF = -3.0 * uF;
+        const double w0 = s->wd[0];
+        const double e0 = (w0 * rho) * (1.0 - k15);
+        nl[0] = (nl[0] - omega * (nl[0] - e0)) + (gp * w0) * m3uF;
+        for (int k = 1; k < q; k += 2) {
+            const double w = s->wd[k];
+            const double cu = s->c[k][0] * v[0] + s->c[k][1] * v[1] + s->c[k][2] * v[2];
+            const double cF = s->c[k][0] * F[0] + s->c[k][1] * F[1] + s->c[k][2] * F[2];
+            const double wr = w * rho;
+            const double ep = wr * ((1.0 + (4.5 * cu) * cu) - k15);
+            const double em = wr * (3.0 * cu);
+            const double sp = 0.5 * (nl[k] + nl[k + 1]);
+            const double sm = 0.5 * (nl[k] - nl[k + 1]);
+            const double a = omega * (sp - ep);
+            const double b = omm * (sm - em);
+            const double Sp = (gp * w) * ((9.0 * cu) * cF + m3uF);
+            const double Sm = (gm * w) * (3.0 * cF);
+            nl[k] = ((nl[k] - a) - b) + (Sp + Sm);
+            nl[k + 1] = ((nl[k + 1] - a) + b) + (Sp - Sm);
+        }
+        return;
+    }
     for (int k = 0; k < q; ++k) {
         const double cu = s->c[k][0] * uu[0] + s->c[k][1] * uu[1] + s->c[k][2] * uu[2];
-        const double neq = (double)s->w[k] * rho *
+        const double neq = s->wd[k] * rho *
                            (1.0 + 3.0 * cu + 4.5 * cu * cu - 1.5 * usq);
         nl[k] = (1.0 - omega) * nl[k] + omega * neq;
     }
@@ -38,6 +70,40 @@ static void FN(collide_node)(const orc_sim* s, R* nl, R rho, const R* ul, R drho
     for (int k = 1; k < q; ++k)
         cu[k] = (float)s->c[k][0] * uu[0] + (float)s->c[k][1] * uu[1] +
                 (float)s->c[k][2] * uu[2];
+    if (s->trt) {
+        /* TRT with a second-order force source; pairs (k, k + 1), k odd.
+         * FP16DEV works on deviations d = f - w: e+ - w = w (drho + rho (4.5cu^2 - 1.5usq)) */
+        const int dev = s->arith == ORC_ARITH_FP16DEV;
+        const float omm = s->omega_m;
+        const float gp = 1.0f - 0.5f * omega, gm = 1.0f - 0.5f * omm;
+        const float hr = 0.5f / rho;
+        float v[3];
+        for (int i = 0; i < 3; ++i) v[i] = ul[i] + s->force[i] * hr;
+        const float vsq = (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2];
+        const float uF = (v[0] * s->force[0] + v[1] * s->force[1]) + v[2] * s->force[2];
+        const float kusq = -1.5f * vsq, base = 1.0f + kusq, m3uF = -3.0f * uF;
+        const float w0 = s->w[0], wr0 = w0 * rho;
+        const float e0 = dev ? fmaf(wr0, kusq, w0 * drho) : wr0 * base;
+        nl[0] = (nl[0] - omega * (nl[0] - e0)) + (gp * w0) * m3uF;
+        for (int k = 1; k < q; k += 2) {
+            const float w = s->w[k], wr = w * rho;
+            const float cuk = (float)s->c[k][0] * v[0] + (float)s->c[k][1] * v[1] + (float)s->c[k][2] * v[2];
+            const float cF = (float)s->c[k][0] * s->force[0] + (float)s->c[k][1] * s->force[1] +
+                             (float)s->c[k][2] * s->force[2];
+            const float t = 4.5f * cuk;
+            const float ep = dev ? fmaf(wr, fmaf(t, cuk, kusq), w * drho) : wr * fmaf(t, cuk, base);
+            const float em = wr * (3.0f * cuk);
+            const float sp = 0.5f * (nl[k] + nl[k + 1]);
+            const float sm = 0.5f * (nl[k] - nl[k + 1]);
+            const float a = omega * (sp - ep);
+            const float b = omm * (sm - em);
+            const float Sp = (gp * w) * fmaf(9.0f * cuk, cF, m3uF);
+            const float Sm = (gm * w) * (3.0f * cF);
+            nl[k] = ((nl[k] - a) - b) + (Sp + Sm);
+            nl[k + 1] = ((nl[k + 1] - a) + b) + (Sp - Sm);
+        }
+        return;
+    }
     if (s->arith == ORC_ARITH_FP16DEV) {
         /* deviation form: nl holds d = f - w;
          * X = 3cu + 4.5cu^2 - 1.5usq, d' = (1-omega) d + w (omega rho X + omega drho) */
@@ -182,7 +248,7 @@ static void FN(noslip)(orc_sim* s) {
                                               s->c[k][1] * (double)ub[1] +
                                               s->c[k][2] * (double)ub[2];
                             n[nb * q + kp] = n[w0 * q + k] -
-                                2.0 * (double)s->w[k] * rho[nb] * cu * (double)s->cs2inv;
+                                2.0 * s->wd[k] * rho[nb] * cu * (double)s->cs2inv;
 #else
                             const float cu = (float)s->c[k][0] * ub[0] +
                                              (float)s->c[k][1] * ub[1] +
@@ -214,7 +280,7 @@ static void FN(noslip)(orc_sim* s) {
                     const double cu = s->c[k][0] * (double)ub[0] + s->c[k][1] * (double)ub[1] +
                                       s->c[k][2] * (double)ub[2];
                     n[nb * q + kp] = n[w0 * q + k] -
-                        2.0 * (double)s->w[k] * rho[nb] * cu * (double)s->cs2inv;
+                        2.0 * s->wd[k] * rho[nb] * cu * (double)s->cs2inv;
 #else
                     const float cu = (float)s->c[k][0] * ub[0] + (float)s->c[k][1] * ub[1] +
                                      (float)s->c[k][2] * ub[2];
@@ -347,7 +413,7 @@ static void FN(init_fields)(orc_sim* s) {
         const double usq = ux * ux + uy * uy + uz * uz;
         for (int k = 0; k < s->q; ++k) {
             const double cu = s->c[k][0] * ux + s->c[k][1] * uy + s->c[k][2] * uz;
-            feq[k] = (double)s->w[k] * (double)s->rho0 *
+            feq[k] = s->wd[k] * (double)s->rho0 *
                      (1.0 + 3.0 * cu + 4.5 * cu * cu - 1.5 * usq);
         }
     }

@@ -62,6 +62,8 @@ def _load_port() -> C.CDLL:
     lib.orc_set_field_f64.argtypes = [C.c_void_p, C.c_int, _dp]
     lib.orc_set_mask.argtypes = [C.c_void_p, C.POINTER(C.c_uint8)]
     lib.orc_set_mask.restype = C.c_int
+    lib.orc_set_trt.argtypes = [C.c_void_p, C.c_float]
+    lib.orc_set_trt.restype = C.c_int
     lib.orc_relaxation.argtypes = [C.c_void_p, _fp, _fp]
     lib.orc_conservation.argtypes = [C.c_void_p, _dp]
     lib.orc_eqlb.argtypes = [C.c_int, C.c_float, _fp, _fp]
@@ -107,10 +109,11 @@ class _Sim:
 
 class Port(_Sim):
     """The C restatement.  mode: MODE_REFERENCE | MODE_NATIVE; arith:
-    ARITH_AVX2 | ARITH_SCALAR | ARITH_FP32; precision 0 = float, 1 = double."""
+    ARITH_AVX2 | ARITH_SCALAR | ARITH_FP32 | ARITH_FP16DEV; precision 0 =
+    float, 1 = double; trt: None (BGK) or the TRT magic parameter."""
 
     def __init__(self, model, nx, ny, nz, nu, rho0, u0, force, rho_solid, face_type, face_vel,
-                 mode=MODE_REFERENCE, arith=ARITH_AVX2, precision=0, mask=None, threads=None):
+                 mode=MODE_REFERENCE, arith=ARITH_AVX2, precision=0, mask=None, threads=None, trt=None):
         self.lib = port_lib()
         self.q = Q_OF[model]
         self.nx, self.ny, self.nz = int(nx), int(ny), int(nz)
@@ -126,6 +129,9 @@ class Port(_Sim):
             assert m.shape == (self.nz, self.ny, self.nx)
             if self.lib.orc_set_mask(self.h, m.ctypes.data_as(C.POINTER(C.c_uint8))) != 0:
                 raise ValueError("mask needs MODE_NATIVE")
+        if trt is not None:   # the TRT magic parameter (0 selects 3/16)
+            if self.lib.orc_set_trt(self.h, float(trt)) != 0:
+                raise ValueError("TRT needs MODE_NATIVE, FP32/FP16DEV arithmetic or double, and tau > 1/2")
 
     def __del__(self):
         h = getattr(self, "h", None)

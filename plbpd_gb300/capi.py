@@ -19,8 +19,10 @@ FACE_NONE, FACE_PERIODIC, FACE_NOSLIP = 0, 1, 2
 FACES = ("east", "west", "north", "south", "up", "down")
 SEMANTICS_REFERENCE, SEMANTICS_NATIVE = 0, 1
 ARITH_REFERENCE, ARITH_FP32 = 0, 1
+COLLISION_BGK, COLLISION_TRT = 0, 1
 STORAGE_FP32, STORAGE_FP16_DEV, STORAGE_FP64 = 0, 1, 2
 FIELD_N, FIELD_NTMP, FIELD_RHO, FIELD_U = 0, 1, 2, 3
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 Q_OF = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27}
 
 
@@ -35,7 +37,7 @@ class Params(C.Structure):
                 ("nu", C.c_float), ("rho0", C.c_float), ("u0", C.c_float * 3), ("force", C.c_float * 3),
                 ("rho_solid", C.c_float), ("face_type", C.c_int32 * 6), ("face_has_vel", C.c_int32 * 6),
                 ("face_vel", (C.c_float * 3) * 6), ("semantics", C.c_int32), ("arith", C.c_int32),
-                ("storage", C.c_int32), ("device", C.c_int32)]
+                ("storage", C.c_int32), ("device", C.c_int32), ("collision", C.c_int32), ("trt_magic", C.c_float)]
 
 
 # (name, restype, argtypes) of every entry point declared in include/plb.h
@@ -75,6 +77,7 @@ _SIGS = [
     ("plb_batch_synchronize", C.c_int, [C.c_void_p]),
     ("plb_batch_destroy", C.c_int, [C.c_void_p]),
     ("plb_batch_cells", C.c_int64, [C.c_void_p]),
+    ("plb_batch_stream_handle", C.c_void_p, [C.c_void_p]),
     ("plb_solve_bytes", C.c_int64, [C.POINTER(Params)]),
     ("plb_server_start", C.c_int, [C.c_int32, C.c_int64, C.c_int32, C.POINTER(C.c_void_p)]),
     ("plb_server_submit", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]),
@@ -144,7 +147,8 @@ def relaxation(nu: float):
 def make_params(model: str, nx: int, ny: int, nz: int, nu: float, rho0: float = 1.0, u0=(0, 0, 0),
                 force=(0, 0, 0), rho_solid: float = 1.0, face_type: dict | None = None,
                 face_vel: dict | None = None, semantics: int = SEMANTICS_REFERENCE,
-                arith: int = ARITH_REFERENCE, storage: int = STORAGE_FP32, device: int = 0) -> Params:
+                arith: int = ARITH_REFERENCE, storage: int = STORAGE_FP32, device: int = 0,
+                collision: int = COLLISION_BGK, trt_magic: float = 0.0) -> Params:
     face_type = face_type or {}
     face_vel = face_vel or {}
     p = Params()
@@ -162,6 +166,7 @@ def make_params(model: str, nx: int, ny: int, nz: int, nu: float, rho0: float = 
             for i in range(3):
                 p.face_vel[f][i] = float(face_vel[name][i])
     p.semantics, p.arith, p.storage, p.device = int(semantics), int(arith), int(storage), int(device)
+    p.collision, p.trt_magic = int(collision), float(trt_magic)
     return p
 
 
@@ -300,3 +305,72 @@ class Batch:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class Request(C.Structure):
+    """plb_request: one solve for the server."""
+    _fields_ = [("params", Params), ("mask", C.c_void_p), ("steps", C.c_int64)]
+
+
+class Server:
+    """The solve server (plb_server_*): submit requests as they arrive, wait,
+    collect rho/u.  Requests use NATIVE semantics."""
+
+    def __init__(self, budget_bytes: int, tick_steps: int = 256, device: int = 0):
+        h = C.c_void_p()
+        check(lib().plb_server_start(int(device), int(budget_bytes), int(tick_steps), C.byref(h)))
+        self.h = h
+        self._dims = {}
+
+    def submit(self, params: Params, steps: int, mask=None) -> int:
+        req = Request()
+        req.params = params
+        req.steps = int(steps)
+        m = None
+        if mask is not None:
+            m = np.ascontiguousarray(mask, dtype=np.uint8)
+            assert m.shape == (int(params.nz), int(params.ny), int(params.nx))
+            req.mask = m.ctypes.data
+        rid = C.c_int64()
+        check(lib().plb_server_submit(self.h, C.byref(req), C.byref(rid)))   # copies the mask
+        self._dims[rid.value] = (int(params.nz) + 2, int(params.ny) + 2, int(params.nx) + 2)
+        return rid.value
+
+    def status(self, rid: int) -> int:
+        st = C.c_int32()
+        check(lib().plb_server_status(self.h, int(rid), C.byref(st)))
+        return st.value
+
+    def wait(self, rid: int, timeout_s: float = 600.0) -> None:
+        check(lib().plb_server_wait(self.h, int(rid), float(timeout_s)))
+
+    def result(self, rid: int):
+        """(rho, u, (t_submit, t_admit, t_done)) of a finished request."""
+        shape = self._dims.pop(int(rid))
+        rho = np.empty(shape + (1,), np.float32)
+        u = np.empty(shape + (3,), np.float32)
+        t = np.zeros(3, np.float64)
+        check(lib().plb_server_result(self.h, int(rid), _ptr(rho), _ptr(u), _ptr(t)))
+        return rho, u, tuple(float(x) for x in t)
+
+    def memory(self):
+        a, b = C.c_int64(), C.c_int64()
+        check(lib().plb_server_memory(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def stop(self) -> None:
+        if getattr(self, "h", None):
+            lib().plb_server_stop(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.stop()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.stop()

@@ -103,6 +103,7 @@ struct plb_solve {
     int q = 0;
     bool native = false;
     int storage = 0;
+    int karith = 0;          // kernel arithmetic: p.arith, or kArithTRT under TRT
     Geo g{};
     CollideParams cp{};
     FaceParams fp{};
@@ -145,11 +146,16 @@ int set_device(const plb_solve* s) {
     return PLB_OK;
 }
 
+// Device memory is stream-ordered (cudaMallocAsync on the solve's stream):
+// destroying a solve then waits for that stream only, where cudaFree would
+// wait for the whole device and stall every other solve running beside it.
+// plb_solve_create synchronizes its stream before returning, so the memory is
+// usable from any stream afterwards.
 int dalloc(plb_solve* s, void** p, size_t bytes) {
-    const cudaError_t e = cudaMalloc(p, bytes);
+    const cudaError_t e = cudaMallocAsync(p, bytes, s->stream);
     if (e != cudaSuccess) {
         *p = nullptr;
-        return fail(PLB_ENOMEM, std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+        return fail(PLB_ENOMEM, std::string("cudaMallocAsync(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
     }
     s->device_bytes += (int64_t)bytes;
     return PLB_OK;
@@ -166,19 +172,36 @@ void release(plb_solve* s) {
     for (void* ptr : {s->f[0], s->f[1], (void*)s->rho, (void*)s->u, (void*)s->consts, (void*)s->types,
                       (void*)s->types_tmp, (void*)s->links, (void*)s->mask_dev, (void*)s->staging, (void*)s->partials,
                       (void*)s->out4})
-        if (ptr) cudaFree(ptr);
+        if (ptr) cudaFreeAsync(ptr, s->stream);
     if (s->out4_host) cudaFreeHost(s->out4_host);
-    if (s->stream) cudaStreamDestroy(s->stream);
+    if (s->stream) {
+        cudaStreamSynchronize(s->stream);
+        cudaStreamDestroy(s->stream);
+    }
     delete s;
 }
 
 // CollisionSRT's parameters (src/CollisionSRT.cpp:14-21).
+// Under TRT also the odd-moment rate, tau_m = magic/(tau - 1/2) + 1/2 in
+// double, and the source factors 1 - omega/2, 1 - omega_m/2 in float.
 void set_collision_params(plb_solve* s, float nu, const float* force) {
     s->p.nu = nu;
     relaxation(nu, &s->cp.tau, &s->cp.omega);
     s->cp.omc = 1.0f - s->cp.omega;
     s->cp.fx = force[0]; s->cp.fy = force[1]; s->cp.fz = force[2];
     for (int i = 0; i < 3; ++i) s->p.force[i] = force[i];
+    if (s->p.collision == PLB_COLLISION_TRT) {
+        const double lam = s->p.trt_magic > 0.0f ? (double)s->p.trt_magic : 3.0 / 16.0;
+        const double tau_m = lam / ((double)s->cp.tau - 0.5) + 0.5;
+        s->cp.omega_m_d = 1.0 / tau_m;
+        s->cp.omega_m = (float)s->cp.omega_m_d;
+    } else {
+        s->cp.omega_m_d = 1.0 / (double)s->cp.tau;
+        s->cp.omega_m = s->cp.omega;
+    }
+    s->cp.gp = 1.0f - 0.5f * s->cp.omega;
+    s->cp.gm = 1.0f - 0.5f * s->cp.omega_m;
+    s->karith = s->p.collision == PLB_COLLISION_TRT ? (int)kArithTRT : (int)s->p.arith;
 }
 
 // Boundary's parameters (src/Boundary.cpp:20-32) and the no-slip launch
@@ -253,6 +276,15 @@ int validate(const plb_params* p) {
         return fail(PLB_EINVAL, "invalid storage");
     if (p->storage != PLB_STORAGE_FP32 && p->semantics != PLB_SEMANTICS_NATIVE)
         return fail(PLB_EUNSUPPORTED, "FP16 and FP64 storage need NATIVE semantics");
+    if (p->collision != PLB_COLLISION_BGK && p->collision != PLB_COLLISION_TRT)
+        return fail(PLB_EINVAL, "invalid collision operator");
+    if (p->collision == PLB_COLLISION_TRT) {
+        if (p->semantics != PLB_SEMANTICS_NATIVE) return fail(PLB_EUNSUPPORTED, "TRT needs NATIVE semantics");
+        if (p->storage == PLB_STORAGE_FP32 && p->arith != PLB_ARITH_FP32)
+            return fail(PLB_EUNSUPPORTED, "TRT with FP32 storage needs PLB_ARITH_FP32");
+        if (!(p->trt_magic >= 0.0f) || p->trt_magic > 1e30f) return fail(PLB_EINVAL, "invalid TRT magic parameter");
+        if (!(3.0f * p->nu + 0.5f > 0.5f)) return fail(PLB_EINVAL, "TRT needs tau > 1/2 (nu > 0)");
+    }
     if (p->semantics == PLB_SEMANTICS_NATIVE) {
         int32_t c[27 * 3];
         tables(p->q, c, nullptr, nullptr);
@@ -275,7 +307,7 @@ int ensure_staging(plb_solve* s, int v) {
     const size_t cells = (size_t)(s->p.nx + 2) * (s->p.ny + 2) * (s->p.nz + 2);
     const size_t need = cells * (size_t)v;
     if (s->staging && s->staging_len >= need) return PLB_OK;
-    if (s->staging) { cudaFree(s->staging); s->device_bytes -= (int64_t)(s->staging_len * sizeof(float)); s->staging = nullptr; }
+    if (s->staging) { cudaFreeAsync(s->staging, s->stream); s->device_bytes -= (int64_t)(s->staging_len * sizeof(float)); s->staging = nullptr; }
     PLB_TRY(dalloc(s, (void**)&s->staging, need * sizeof(float)));
     s->staging_len = need;
     return PLB_OK;
@@ -327,7 +359,7 @@ int ref_materialize_fields(plb_solve* s) {
 
 // ---- NATIVE semantics ------------------------------------------------------
 int nat_one_step(plb_solve* s) {
-    PLB_KERNEL(nat_fused_step(s->q, s->storage, s->p.arith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
+    PLB_KERNEL(nat_fused_step(s->q, s->storage, s->karith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
                               s->f[1 - s->cur], s->types, s->stream));
     s->cur = 1 - s->cur;
     return PLB_OK;
@@ -395,7 +427,7 @@ int march(plb_solve* s, int64_t n) {
     }
     int64_t done = 0;
     if (!s->post) {
-        PLB_KERNEL(nat_collide_raw(s->q, s->storage, s->p.arith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
+        PLB_KERNEL(nat_collide_raw(s->q, s->storage, s->karith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
                                    s->f[1 - s->cur], s->rho, s->u, s->types, s->stream));
         s->cur = 1 - s->cur;
         s->post = true;
@@ -549,6 +581,8 @@ int plb_set_relaxation(plb_solve* s, float nu, const float* force3) {
     if (!s || !force3) return fail(PLB_EINVAL, "null argument");
     if (s->p.nu == nu && s->p.force[0] == force3[0] && s->p.force[1] == force3[1] && s->p.force[2] == force3[2])
         return PLB_OK;
+    if (s->p.collision == PLB_COLLISION_TRT && !(3.0f * nu + 0.5f > 0.5f))
+        return fail(PLB_EINVAL, "TRT needs tau > 1/2 (nu > 0)");
     PLB_TRY(set_device(s));
     PLB_TRY(sync(s));
     set_collision_params(s, nu, force3);
@@ -792,7 +826,7 @@ struct plb_batch {
     int q = 0, storage = 0, arith = 0, device = 0;
     cudaStream_t stream = nullptr;
     BatchDomain* d_doms = nullptr;
-    int4* d_tiles = nullptr;   // warp tasks (domain, y, z, x0)
+    int4* d_tiles = nullptr;   // warp tasks (domain, z, first node of the plane, 0)
     int ntiles = 0;
     int blocks = 0;
     int64_t cells = 0;
@@ -807,9 +841,12 @@ namespace {
 void batch_release(plb_batch* b) {
     if (!b) return;
     if (b->graph) cudaGraphExecDestroy(b->graph);
-    if (b->d_doms) cudaFree(b->d_doms);
-    if (b->d_tiles) cudaFree(b->d_tiles);
-    if (b->stream) cudaStreamDestroy(b->stream);
+    if (b->d_doms) cudaFreeAsync(b->d_doms, b->stream);
+    if (b->d_tiles) cudaFreeAsync(b->d_tiles, b->stream);
+    if (b->stream) {
+        cudaStreamSynchronize(b->stream);
+        cudaStreamDestroy(b->stream);
+    }
     delete b;
 }
 
@@ -823,11 +860,11 @@ int batch_prepare(plb_batch* b, int64_t* consumed) {
     if (!any_raw) return PLB_OK;
     for (plb_solve* s : b->solves) {
         if (!s->post) {
-            PLB_KERNEL(nat_collide_raw(s->q, s->storage, s->p.arith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
+            PLB_KERNEL(nat_collide_raw(s->q, s->storage, s->karith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
                                        s->f[1 - s->cur], s->rho, s->u, s->types, b->stream));
             s->post = true;
         } else {
-            PLB_KERNEL(nat_fused_step(s->q, s->storage, s->p.arith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
+            PLB_KERNEL(nat_fused_step(s->q, s->storage, s->karith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
                                       s->f[1 - s->cur], s->types, b->stream));
         }
         s->cur = 1 - s->cur;
@@ -886,7 +923,7 @@ int plb_batch_create(int32_t n, plb_solve* const* solves, plb_batch** out) {
         const plb_solve* s = solves[i];
         if (!s) return fail(PLB_EINVAL, "null solve");
         if (!s->native) return fail(PLB_EUNSUPPORTED, "batches need NATIVE semantics");
-        if (s->q != s0->q || s->storage != s0->storage || s->p.arith != s0->p.arith || s->p.device != s0->p.device)
+        if (s->q != s0->q || s->storage != s0->storage || s->karith != s0->karith || s->p.device != s0->p.device)
             return fail(PLB_EINVAL, "batch members must share lattice, storage, arithmetic and device");
         if (s->storage == PLB_STORAGE_FP64) return fail(PLB_EUNSUPPORTED, "FP64 storage is not batched");
         if ((long long)s->g.ys * s->g.ny * s->g.nz >= (1ll << 31))
@@ -894,7 +931,7 @@ int plb_batch_create(int32_t n, plb_solve* const* solves, plb_batch** out) {
     }
     plb_batch* b = new plb_batch();
     b->solves.assign(solves, solves + n);
-    b->q = s0->q; b->storage = s0->storage; b->arith = s0->p.arith; b->device = s0->p.device;
+    b->q = s0->q; b->storage = s0->storage; b->arith = s0->karith; b->device = s0->p.device;
     b->graph_steps = graph_steps_default();
     b->h_doms.resize(n);
     if (cudaSetDevice(b->device) != cudaSuccess) { batch_release(b); return fail(PLB_ECUDA, "cudaSetDevice"); }
@@ -905,9 +942,9 @@ int plb_batch_create(int32_t n, plb_solve* const* solves, plb_batch** out) {
     std::vector<int4> tiles;
     for (int i = 0; i < n; ++i) {
         const Geo& g = solves[i]->g;
+        const int plane = g.nx * g.ny;   // nodes of one z plane, x fastest
         for (int z = 0; z < g.nz; ++z)
-            for (int y = 0; y < g.ny; ++y)
-                for (int x0 = 0; x0 < g.nx; x0 += 32) tiles.push_back(make_int4(i, y, z, x0));
+            for (int i0 = 0; i0 < plane; i0 += 32) tiles.push_back(make_int4(i, z, i0, 0));
         b->cells += g.cells();
     }
     b->ntiles = (int)tiles.size();
@@ -916,12 +953,15 @@ int plb_batch_create(int32_t n, plb_solve* const* solves, plb_batch** out) {
     for (int i = 0; i < n; ++i) b->moving |= solves[i]->np.moving != 0;
     const int per_sm = nat_batch_blocks_per_sm(b->q, b->storage, b->arith, b->moving);
     b->blocks = (dev_sms > 0 ? dev_sms : 1) * (per_sm > 0 ? per_sm : 1);
-    if (cudaMalloc(&b->d_doms, n * sizeof(BatchDomain)) != cudaSuccess ||
-        cudaMalloc(&b->d_tiles, tiles.size() * sizeof(int4)) != cudaSuccess) {
+    // stream-ordered, like a solve's memory
+    if (cudaMallocAsync(&b->d_doms, n * sizeof(BatchDomain), b->stream) != cudaSuccess ||
+        cudaMallocAsync(&b->d_tiles, tiles.size() * sizeof(int4), b->stream) != cudaSuccess) {
         batch_release(b);
         return fail(PLB_ENOMEM, "batch tables");
     }
-    if (cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess) {
+    if (cudaMemcpyAsync(b->d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, b->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(b->stream) != cudaSuccess) {
         batch_release(b);
         return fail(PLB_ECUDA, "batch tile upload");
     }
@@ -973,5 +1013,7 @@ int plb_batch_destroy(plb_batch* b) {
 }
 
 int64_t plb_batch_cells(const plb_batch* b) { return b ? b->cells : 0; }
+
+void* plb_batch_stream_handle(plb_batch* b) { return b ? (void*)b->stream : nullptr; }
 
 }  // extern "C"

@@ -58,8 +58,9 @@ int ref_moments(int q, const Geo& g, const float* n, float* rho, float* u, cudaS
 int ref_reset(const Geo& g, const FaceParams& fp, bool velocity, bool density, float* rho,
               float* u, cudaStream_t st);
 
-// ---- NATIVE semantics (kernels_native.cu) ---------------------------------
-// storage: 0 = FP32, 1 = FP16 deviations f - w.
+// ---- NATIVE semantics (kernels_native.cu; TRT in kernels_trt.cu) -----------
+// storage: 0 = FP32, 1 = FP16 deviations f - w, 2 = FP64.  arith: kArith*;
+// kArithTRT selects the two-relaxation-time operator for any storage.
 // Collision of a RAW state (n in `src`, rho/u fields), result P into `dst`.
 int nat_collide_raw(int q, int storage, int arith, bool has_mask, const Geo& g,
                     const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
@@ -91,8 +92,8 @@ struct BatchDomain {
     const uint8_t* types;
     void* f[2];
 };
-// A task is one warp's work: up to 32 nodes of one row of one domain,
-// (domain index, y, z, first x).
+// A task is one warp's work: up to 32 consecutive nodes of one z plane of
+// one domain, (domain index, z, first node of the plane in x-fastest order, 0).
 // One launch advances every domain by one step, reading f[parity] and
 // writing f[parity ^ 1]; `blocks` resident blocks walk the task list.
 // `moving`: some member has a moving wall.
@@ -101,6 +102,16 @@ int nat_batch_step(int q, int storage, int arith, bool moving, const BatchDomain
 // Resident blocks per SM of the batch kernel (for sizing the grid).
 int nat_batch_blocks_per_sm(int q, int storage, int arith, bool moving);
 constexpr int kBatchTile = 128;
+
+// The TRT instantiations behind the functions above (kernels_trt.cu).
+int nat_fused_step_trt(int q, int storage, bool has_mask, const Geo& g, const CollideParams& cp,
+                       const NativeParams& np, const void* src, void* dst, const uint8_t* types, cudaStream_t st);
+int nat_collide_raw_trt(int q, int storage, bool has_mask, const Geo& g, const CollideParams& cp,
+                        const NativeParams& np, const void* src, void* dst, const float* rho, const float* u,
+                        const uint8_t* types, cudaStream_t st);
+int nat_batch_blocks_per_sm_trt(int q, int storage, bool moving);
+int nat_batch_step_trt(int q, int storage, bool moving, const BatchDomain* doms, const int4* tiles, int ntiles,
+                       int parity, int blocks, cudaStream_t st);
 
 // ---- shared (kernels_util.cu) ----------------------------------------------
 // Every node of the box (halo included): rho0, u0, n = feq, ntmp = 0.

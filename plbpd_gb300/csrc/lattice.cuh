@@ -83,6 +83,15 @@ __host__ __device__ constexpr float weight(int k) {
             : speed2<Q>(k) == 2 ? float(1. / 54.) : float(1. / 216.));
 }
 
+// The exact weights in double, for FP64 storage: the float weights sum to
+// 1 + O(1e-8), which an FP64 run would add to the mass at every collision.
+template <int Q>
+__host__ __device__ constexpr double weight_d(int k) {
+    return Q == 9 ? (speed2<Q>(k) == 0 ? 4. / 9. : speed2<Q>(k) == 1 ? 1. / 9. : 1. / 36.)
+         : Q == 19 ? (speed2<Q>(k) == 0 ? 1. / 3. : speed2<Q>(k) == 1 ? 1. / 18. : 1. / 36.)
+         : (speed2<Q>(k) == 0 ? 8. / 27. : speed2<Q>(k) == 1 ? 2. / 27. : speed2<Q>(k) == 2 ? 1. / 54. : 1. / 216.);
+}
+
 // ---------------------------------------------------------------------------
 // device layout
 // ---------------------------------------------------------------------------
@@ -118,9 +127,15 @@ struct Geo {
 struct CollideParams {
     float tau, omega, omc;    // omc = 1.0f - omega (float subtraction)
     float fx, fy, fz;         // body force
+    // TRT: odd-moment rate 1/tau_m (float and double) and the source factors
+    // gp = 1 - omega/2, gm = 1 - omega_m/2 (float arithmetic)
+    float omega_m, gp, gm;
+    double omega_m_d;
 };
 
-enum Arith : int { kArithReference = 0, kArithFP32 = 1 };
+// Kernel arithmetic: plbpd's (FP32 body + FP64 tail), FP32 only, or the
+// two-relaxation-time operator (FP32 arithmetic).
+enum Arith : int { kArithReference = 0, kArithFP32 = 1, kArithTRT = 2 };
 
 // Sums of one node in direction order: r = sum f_k, j = sum c_k f_k.  c is
 // -1, 0 or 1, so f*c is exact and adding the zero products leaves every

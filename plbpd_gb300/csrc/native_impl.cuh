@@ -1,0 +1,762 @@
+// Native-semantics kernel templates and their host-side dispatch, shared by
+// kernels_native.cu (BGK instantiations) and kernels_trt.cu (TRT).
+//
+// The device holds P, the post-collision populations of the previous step.
+// A step at node x gathers n[x][k] = P[x - c_k][k] (periodic axes wrap), or,
+// when x - c_k is solid, the bounce-back value P[x][rev k] that node x itself
+// stored with the moving-wall term already applied; then it computes the
+// moments, collides and stores P[x][k] at its own node.  Reads of a shifted
+// row are misaligned by one element, writes are whole aligned sectors.
+//
+// The bounce-back is plbpd's no-slip rule (src/Boundary.cpp:189-221) for a
+// fluid node next to a solid one:
+//   n[x][rev k] = P[x][k] - 2 w_k rho[x] (c_k . u_b) / c_s^2,  x + c_k solid,
+// with rho[x] the density node x collided with -- available in registers when
+// P[x][k] is stored, so the term is applied on the store side.
+//
+// Storage (template parameter ST):
+//   0  FP32 populations, plbpd's FP32 arithmetic (or FP32-only, ARITH)
+//   1  FP16 deviations d_k = f_k - w_k, arithmetic in FP32 in deviation form
+//   2  FP64 populations and FP64 arithmetic: the reference run of the same
+//      method that reduced-precision runs are measured against
+#pragma once
+
+#include <type_traits>
+
+#include "engine.h"
+
+namespace plb {
+namespace {
+
+constexpr int kBlockX = 128;
+
+template <int ST> struct Store;
+template <> struct Store<0> {
+    using T = float;
+    using R = float;
+    __device__ static __forceinline__ float ld(const float* p, long long i) { return __ldg(p + i); }
+    __device__ static __forceinline__ void st(float* p, long long i, float v) { __stcs(p + i, v); }
+};
+template <> struct Store<1> {
+    using T = __half;
+    using R = float;
+    __device__ static __forceinline__ float ld(const __half* p, long long i) { return __half2float(__ldg(p + i)); }
+    __device__ static __forceinline__ void st(__half* p, long long i, float v) {
+        __stcs(reinterpret_cast<unsigned short*>(p) + i, __half_as_ushort(__float2half_rn(v)));
+    }
+};
+template <> struct Store<2> {
+    using T = double;
+    using R = double;
+    __device__ static __forceinline__ double ld(const double* p, long long i) { return __ldg(p + i); }
+    __device__ static __forceinline__ void st(double* p, long long i, double v) { __stcs(p + i, v); }
+};
+
+// Neighbour index helper: element offsets of x-1, x, x+1 (and y, z) with the
+// periodic axes wrapped.  A fluid node never has a neighbour outside the box
+// along a walled axis, because the wall layer in between is solid.
+struct Nbr {
+    long long xo[3], yo[3], zo[3];
+    __device__ __forceinline__ Nbr(const Geo& g, int x, int y, int z) {
+        const int xm = (x == 0 && g.wrap_x) ? g.nx - 1 : x - 1;
+        const int xp = (x == g.nx - 1 && g.wrap_x) ? 0 : x + 1;
+        const int ym = (y == 0 && g.wrap_y) ? g.ny - 1 : y - 1;
+        const int yp = (y == g.ny - 1 && g.wrap_y) ? 0 : y + 1;
+        const int zm = (z == 0 && g.wrap_z) ? g.nz - 1 : z - 1;
+        const int zp = (z == g.nz - 1 && g.wrap_z) ? 0 : z + 1;
+        xo[0] = xm + g.xoff; xo[1] = x + g.xoff; xo[2] = xp + g.xoff;
+        yo[0] = (long long)ym * g.ys; yo[1] = (long long)y * g.ys; yo[2] = (long long)yp * g.ys;
+        zo[0] = (long long)zm * g.zs; zo[1] = (long long)z * g.zs; zo[2] = (long long)zp * g.zs;
+    }
+    // node at x + s*c_k, s = +1 (downstream) or -1 (upstream)
+    template <int Q>
+    __device__ __forceinline__ long long at(int k, int s) const {
+        return zo[1 + s * Lattice<Q>::cz(k)] + yo[1 + s * Lattice<Q>::cy(k)] + xo[1 + s * Lattice<Q>::cx(k)];
+    }
+};
+
+// ---- FP16 storage: deviation form -----------------------------------------
+// d_k = f_k - w_k, drho = sum d_k, rho = 1 + drho, and
+//   f_eq,k - w_k = w_k (drho + rho X_k),  X_k = 3 cu + 4.5 cu^2 - 1.5 usq,
+//   d'_k = (1 - omega) d_k + omega (f_eq,k - w_k).
+// Written for few operations: per weight class A = w (omega rho) and
+// B = w (omega drho), then per direction
+//   X = fma(cu, fma(4.5, cu, 3), -1.5 usq),  d' = fma(1 - omega, d, fma(A, X, B)).
+template <int Q>
+__device__ __forceinline__ void collide_node_dev(float (&d)[Q], float drho, float rho, float ux, float uy,
+                                                 float uz, const CollideParams& P) {
+    const float tr = __fdiv_rn(P.tau, rho);
+    const float vx = __fadd_rn(ux, __fmul_rn(P.fx, tr));
+    const float vy = __fadd_rn(uy, __fmul_rn(P.fy, tr));
+    const float vz = __fadd_rn(uz, __fmul_rn(P.fz, tr));
+    const float usq = __fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz));
+    const float kusq = __fmul_rn(-1.5f, usq);
+    const float orho = __fmul_rn(P.omega, rho);
+    const float odrho = __fmul_rn(P.omega, drho);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        const float cu = (k == 0) ? 0.0f : dot_c<Q>(k, vx, vy, vz);
+        const float A = __fmul_rn(weight<Q>(k), orho);     // shared by a weight class after CSE
+        const float B = __fmul_rn(weight<Q>(k), odrho);
+        const float X = __fmaf_rn(cu, __fmaf_rn(4.5f, cu, 3.0f), kusq);
+        d[k] = __fmaf_rn(P.omc, d[k], __fmaf_rn(A, X, B));
+    }
+}
+
+template <int Q>
+__device__ __forceinline__ void node_moments_dev(const float (&d)[Q], float& drho, float& rho, float& ux,
+                                                 float& uy, float& uz) {
+    float jx, jy, jz;
+    node_sums<Q>(d, drho, jx, jy, jz);
+    rho = __fadd_rn(1.0f, drho);
+    const float rinv = __fdiv_rn(1.0f, rho);
+    ux = __fmul_rn(jx, rinv);
+    uy = __fmul_rn(jy, rinv);
+    uz = __fmul_rn(jz, rinv);
+}
+
+// ---- FP64 storage: the same method in double ---------------------------------
+// With the exact weights in double (weight_d).
+// Op order: u_eq = u + F (tau/rho); usq = (ux^2 + uy^2) + uz^2;
+// neq = (w rho)(((1 + 3cu) + (4.5cu)cu) - 1.5usq); n = (1-omega) n + omega neq.
+template <int Q>
+__device__ __forceinline__ double dot_c_d(int k, double ux, double uy, double uz) {
+    double acc = 0.0;
+    bool any = false;
+    if (Lattice<Q>::cx(k) != 0) { acc = Lattice<Q>::cx(k) > 0 ? ux : -ux; any = true; }
+    if (Lattice<Q>::cy(k) != 0) {
+        const double t = Lattice<Q>::cy(k) > 0 ? uy : -uy;
+        acc = any ? __dadd_rn(acc, t) : t;
+        any = true;
+    }
+    if (Lattice<Q>::cz(k) != 0) {
+        const double t = Lattice<Q>::cz(k) > 0 ? uz : -uz;
+        acc = any ? __dadd_rn(acc, t) : t;
+    }
+    return acc;
+}
+
+template <int Q>
+__device__ __forceinline__ void node_moments_d(const double (&f)[Q], double& rho, double& ux, double& uy,
+                                               double& uz) {
+    double r = 0.0, jx = 0.0, jy = 0.0, jz = 0.0;
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        r = __dadd_rn(r, f[k]);
+        if (Lattice<Q>::cx(k) > 0) jx = __dadd_rn(jx, f[k]);
+        if (Lattice<Q>::cx(k) < 0) jx = __dsub_rn(jx, f[k]);
+        if (Lattice<Q>::cy(k) > 0) jy = __dadd_rn(jy, f[k]);
+        if (Lattice<Q>::cy(k) < 0) jy = __dsub_rn(jy, f[k]);
+        if (Lattice<Q>::cz(k) > 0) jz = __dadd_rn(jz, f[k]);
+        if (Lattice<Q>::cz(k) < 0) jz = __dsub_rn(jz, f[k]);
+    }
+    const double rinv = __ddiv_rn(1.0, r);
+    rho = r;
+    ux = __dmul_rn(jx, rinv);
+    uy = __dmul_rn(jy, rinv);
+    uz = __dmul_rn(jz, rinv);
+}
+
+template <int Q>
+__device__ __forceinline__ void collide_node_d(double (&f)[Q], double rho, double ux, double uy, double uz,
+                                               const CollideParams& P) {
+    const double tau = (double)P.tau;
+    const double omega = __ddiv_rn(1.0, tau);
+    const double omc = __dsub_rn(1.0, omega);
+    const double tr = __ddiv_rn(tau, rho);
+    const double vx = __dadd_rn(ux, __dmul_rn((double)P.fx, tr));
+    const double vy = __dadd_rn(uy, __dmul_rn((double)P.fy, tr));
+    const double vz = __dadd_rn(uz, __dmul_rn((double)P.fz, tr));
+    const double usq = __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz));
+    const double k15 = __dmul_rn(1.5, usq);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        const double cu = (k == 0) ? 0.0 : dot_c_d<Q>(k, vx, vy, vz);
+        double br = __dadd_rn(1.0, __dmul_rn(3.0, cu));
+        br = __dadd_rn(br, __dmul_rn(__dmul_rn(4.5, cu), cu));
+        br = __dsub_rn(br, k15);
+        const double neq = __dmul_rn(__dmul_rn(weight_d<Q>(k), rho), br);
+        f[k] = __dadd_rn(__dmul_rn(omc, f[k]), __dmul_rn(omega, neq));
+    }
+}
+
+// ---- TRT ----------------------------------------------------------------------
+// Two relaxation times with a second-order force source (the oracle's
+// orc_set_trt states the method); pairs (k, k + 1) with k odd are opposite
+// directions.  DEV: populations are deviations d = f - w (FP16 storage), so
+// the even equilibrium enters as e+ - w = w (drho + rho (4.5cu^2 - 1.5usq)).
+// Op order, FP32:
+//   hr = 0.5/rho; v = u + F hr; vsq = (vx^2 + vy^2) + vz^2; uF = (vx Fx + vy Fy) + vz Fz
+//   kusq = -1.5 vsq; base = 1 + kusq; m3uF = -3 uF
+//   e0 = (w0 rho) base | fma(w0 rho, kusq, w0 drho);  n0 = (n0 - om (n0 - e0)) + (gp w0) m3uF
+//   per pair: t = 4.5 cu; e+ = (w rho) fma(t, cu, base) | fma(w rho, fma(t, cu, kusq), w drho)
+//     e- = (w rho)(3 cu); s+ = 0.5 (nk + nr); s- = 0.5 (nk - nr)
+//     a = om (s+ - e+); b = omm (s- - e-); S+ = (gp w) fma(9 cu, cF, m3uF); S- = (gm w)(3 cF)
+//     nk = ((nk - a) - b) + (S+ + S-); nr = ((nr - a) + b) + (S+ - S-)
+template <int Q, bool DEV>
+__device__ __forceinline__ void collide_node_trt(float (&f)[Q], float drho, float rho, float ux, float uy, float uz,
+                                                 const CollideParams& P) {
+    const float hr = __fdiv_rn(0.5f, rho);
+    const float vx = __fadd_rn(ux, __fmul_rn(P.fx, hr));
+    const float vy = __fadd_rn(uy, __fmul_rn(P.fy, hr));
+    const float vz = __fadd_rn(uz, __fmul_rn(P.fz, hr));
+    const float vsq = __fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz));
+    const float uF = __fadd_rn(__fadd_rn(__fmul_rn(vx, P.fx), __fmul_rn(vy, P.fy)), __fmul_rn(vz, P.fz));
+    const float kusq = __fmul_rn(-1.5f, vsq);
+    const float base = __fadd_rn(1.0f, kusq);
+    const float m3uF = __fmul_rn(-3.0f, uF);
+    const float om = P.omega, omm = P.omega_m;
+    {
+        const float w0 = weight<Q>(0), wr0 = __fmul_rn(w0, rho);
+        const float e0 = DEV ? __fmaf_rn(wr0, kusq, __fmul_rn(w0, drho)) : __fmul_rn(wr0, base);
+        f[0] = __fadd_rn(__fsub_rn(f[0], __fmul_rn(om, __fsub_rn(f[0], e0))), __fmul_rn(__fmul_rn(P.gp, w0), m3uF));
+    }
+#pragma unroll
+    for (int k = 1; k < Q; k += 2) {
+        const float w = weight<Q>(k), wr = __fmul_rn(w, rho);
+        const float cu = dot_c<Q>(k, vx, vy, vz);
+        const float cF = dot_c<Q>(k, P.fx, P.fy, P.fz);
+        const float t = __fmul_rn(4.5f, cu);
+        const float ep = DEV ? __fmaf_rn(wr, __fmaf_rn(t, cu, kusq), __fmul_rn(w, drho))
+                             : __fmul_rn(wr, __fmaf_rn(t, cu, base));
+        const float em = __fmul_rn(wr, __fmul_rn(3.0f, cu));
+        const float sp = __fmul_rn(0.5f, __fadd_rn(f[k], f[k + 1]));
+        const float sm = __fmul_rn(0.5f, __fsub_rn(f[k], f[k + 1]));
+        const float a = __fmul_rn(om, __fsub_rn(sp, ep));
+        const float b = __fmul_rn(omm, __fsub_rn(sm, em));
+        const float Sp = __fmul_rn(__fmul_rn(P.gp, w), __fmaf_rn(__fmul_rn(9.0f, cu), cF, m3uF));
+        const float Sm = __fmul_rn(__fmul_rn(P.gm, w), __fmul_rn(3.0f, cF));
+        const float nk = __fadd_rn(__fsub_rn(__fsub_rn(f[k], a), b), __fadd_rn(Sp, Sm));
+        const float nr = __fadd_rn(__fadd_rn(__fsub_rn(f[k + 1], a), b), __fsub_rn(Sp, Sm));
+        f[k] = nk;
+        f[k + 1] = nr;
+    }
+}
+
+// The same in double (FP64 storage): omega = 1/tau and gp = 1 - omega/2 in
+// double, omm = omega_m_d, gm = 1 - omm/2; e+ = (w rho)((1 + (4.5cu)cu) - 1.5vsq),
+// S+ = (gp w)((9cu) cF + m3uF); otherwise the FP32 order.
+template <int Q>
+__device__ __forceinline__ void collide_node_trt_d(double (&f)[Q], double rho, double ux, double uy, double uz,
+                                                   const CollideParams& P) {
+    const double om = __ddiv_rn(1.0, (double)P.tau), omm = P.omega_m_d;
+    const double gp = __dsub_rn(1.0, __dmul_rn(0.5, om)), gm = __dsub_rn(1.0, __dmul_rn(0.5, omm));
+    const double Fx = P.fx, Fy = P.fy, Fz = P.fz;
+    const double hr = __ddiv_rn(0.5, rho);
+    const double vx = __dadd_rn(ux, __dmul_rn(Fx, hr));
+    const double vy = __dadd_rn(uy, __dmul_rn(Fy, hr));
+    const double vz = __dadd_rn(uz, __dmul_rn(Fz, hr));
+    const double vsq = __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz));
+    const double uF = __dadd_rn(__dadd_rn(__dmul_rn(vx, Fx), __dmul_rn(vy, Fy)), __dmul_rn(vz, Fz));
+    const double k15 = __dmul_rn(1.5, vsq), m3uF = __dmul_rn(-3.0, uF);
+    {
+        const double w0 = weight_d<Q>(0);
+        const double e0 = __dmul_rn(__dmul_rn(w0, rho), __dsub_rn(1.0, k15));
+        f[0] = __dadd_rn(__dsub_rn(f[0], __dmul_rn(om, __dsub_rn(f[0], e0))), __dmul_rn(__dmul_rn(gp, w0), m3uF));
+    }
+#pragma unroll
+    for (int k = 1; k < Q; k += 2) {
+        const double w = weight_d<Q>(k), wr = __dmul_rn(w, rho);
+        const double cu = dot_c_d<Q>(k, vx, vy, vz);
+        const double cF = dot_c_d<Q>(k, Fx, Fy, Fz);
+        const double ep = __dmul_rn(wr, __dsub_rn(__dadd_rn(1.0, __dmul_rn(__dmul_rn(4.5, cu), cu)), k15));
+        const double em = __dmul_rn(wr, __dmul_rn(3.0, cu));
+        const double sp = __dmul_rn(0.5, __dadd_rn(f[k], f[k + 1]));
+        const double sm = __dmul_rn(0.5, __dsub_rn(f[k], f[k + 1]));
+        const double a = __dmul_rn(om, __dsub_rn(sp, ep));
+        const double b = __dmul_rn(omm, __dsub_rn(sm, em));
+        const double Sp = __dmul_rn(__dmul_rn(gp, w), __dadd_rn(__dmul_rn(__dmul_rn(9.0, cu), cF), m3uF));
+        const double Sm = __dmul_rn(__dmul_rn(gm, w), __dmul_rn(3.0, cF));
+        const double nk = __dadd_rn(__dsub_rn(__dsub_rn(f[k], a), b), __dadd_rn(Sp, Sm));
+        const double nr = __dadd_rn(__dadd_rn(__dsub_rn(f[k + 1], a), b), __dsub_rn(Sp, Sm));
+        f[k] = nk;
+        f[k + 1] = nr;
+    }
+}
+
+// ---- per storage: moments + collision, and the moving-wall correction ---------
+// Collision of one node from its moments, per storage and operator.
+template <int Q, int ST, int ARITH>
+__device__ __forceinline__ void collide_any(typename Store<ST>::R (&f)[Q], typename Store<ST>::R rho,
+                                            typename Store<ST>::R ux, typename Store<ST>::R uy,
+                                            typename Store<ST>::R uz, float drho, const CollideParams& cp) {
+    if constexpr (ST == 0) {
+        if constexpr (ARITH == kArithTRT) collide_node_trt<Q, false>(f, 0.0f, rho, ux, uy, uz, cp);
+        else collide_node<Q, ARITH>(f, rho, ux, uy, uz, cp);
+    } else if constexpr (ST == 1) {
+        if constexpr (ARITH == kArithTRT) collide_node_trt<Q, true>(f, drho, rho, ux, uy, uz, cp);
+        else collide_node_dev<Q>(f, drho, rho, ux, uy, uz, cp);
+    } else {
+        if constexpr (ARITH == kArithTRT) collide_node_trt_d<Q>(f, rho, ux, uy, uz, cp);
+        else collide_node_d<Q>(f, rho, ux, uy, uz, cp);
+    }
+}
+
+template <int Q, int ST, int ARITH>
+__device__ __forceinline__ void update_node(typename Store<ST>::R (&f)[Q], typename Store<ST>::R& rho,
+                                            const CollideParams& cp) {
+    if constexpr (ST == 0) {
+        float ux, uy, uz;
+        node_moments<Q>(f, rho, ux, uy, uz);
+        collide_any<Q, ST, ARITH>(f, rho, ux, uy, uz, 0.0f, cp);
+    } else if constexpr (ST == 1) {
+        float drho, ux, uy, uz;
+        node_moments_dev<Q>(f, drho, rho, ux, uy, uz);
+        collide_any<Q, ST, ARITH>(f, rho, ux, uy, uz, drho, cp);
+    } else {
+        double ux, uy, uz;
+        node_moments_d<Q>(f, rho, ux, uy, uz);
+        collide_any<Q, ST, ARITH>(f, rho, ux, uy, uz, 0.0f, cp);
+    }
+}
+
+template <int Q, int ST>
+__device__ __forceinline__ void moments_any(const typename Store<ST>::R (&f)[Q], typename Store<ST>::R& rho,
+                                            typename Store<ST>::R& ux, typename Store<ST>::R& uy,
+                                            typename Store<ST>::R& uz) {
+    if constexpr (ST == 0) node_moments<Q>(f, rho, ux, uy, uz);
+    else if constexpr (ST == 1) { float drho; node_moments_dev<Q>(f, drho, rho, ux, uy, uz); }
+    else node_moments_d<Q>(f, rho, ux, uy, uz);
+}
+
+// v - 2 w_k rho (c_k . u_b) / c_s^2, in the storage's arithmetic
+template <int Q, int ST>
+__device__ __forceinline__ typename Store<ST>::R wall_corrected(int k, typename Store<ST>::R v,
+                                                                typename Store<ST>::R rho, const float* ub,
+                                                                float cs2inv) {
+    if constexpr (ST == 2) {
+        const double cu = __dadd_rn(__dadd_rn(__dmul_rn((double)Lattice<Q>::cx(k), (double)ub[0]),
+                                              __dmul_rn((double)Lattice<Q>::cy(k), (double)ub[1])),
+                                    __dmul_rn((double)Lattice<Q>::cz(k), (double)ub[2]));
+        const double t = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(2.0, weight_d<Q>(k)), rho), cu), (double)cs2inv);
+        return __dsub_rn(v, t);
+    } else {
+        return __fsub_rn(v, wall_term<Q>(k, rho, dot_c_full<Q>(k, ub), cs2inv));
+    }
+}
+
+// Stores the collided populations of a fluid node; a direction that points
+// into a solid node becomes the bounce-back slot and carries the moving-wall
+// term (src/Boundary.cpp:215-217).
+template <int Q, int ST, bool MASK, bool MOVING = true>
+__device__ __forceinline__ void store_node(typename Store<ST>::T* __restrict__ dst, const Geo& g,
+                                           const NativeParams& np, const uint8_t* __restrict__ types,
+                                           uint32_t links, const Nbr& nb, long long node,
+                                           typename Store<ST>::R rho, const typename Store<ST>::R (&f)[Q]) {
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        typename Store<ST>::R v = f[k];
+        // a resting solid adds nothing (the term is a signed zero)
+        if (MASK && MOVING && k != 0 && np.moving && ((links >> k) & 1u)) {
+            const uint8_t t = __ldg(types + nb.at<Q>(k, +1));
+            v = wall_corrected<Q, ST>(k, v, rho, np.vel[t & kVelMask], np.cs2inv);
+        }
+        Store<ST>::st(dst, k * g.ks + node, v);
+    }
+}
+
+// The solid-link mask of a node (0 for nodes away from solids).
+template <bool MASK>
+__device__ __forceinline__ uint32_t links_of(const uint8_t t, const uint32_t* __restrict__ links, long long node) {
+    return (MASK && (t & kNearSolid)) ? __ldg(links + node) : 0u;
+}
+
+// Gathers n[x][*] from P (streaming plus bounce-back).  `links` bit k is set
+// when x + c_k is solid, so the source x - c_k is solid when bit rev(k) is.
+template <int Q, int ST, bool MASK>
+__device__ __forceinline__ void gather_node(const typename Store<ST>::T* __restrict__ src, const Geo& g,
+                                            uint32_t links, const Nbr& nb, long long node,
+                                            typename Store<ST>::R (&f)[Q]) {
+    // every source is inside the box (a solid source is a node too), so the
+    // streaming loads are unconditional; bounce-back directions are then
+    // replaced by the node's own reversed slot
+#pragma unroll
+    for (int k = 0; k < Q; ++k) f[k] = Store<ST>::ld(src, k * g.ks + nb.at<Q>(k, -1));
+    if (MASK && links) {
+#pragma unroll
+        for (int k = 1; k < Q; ++k)
+            if ((links >> rev_of(k)) & 1u) f[k] = Store<ST>::ld(src, rev_of(k) * g.ks + node);
+    }
+}
+
+// ---------------------------------------------------------------------------
+template <int Q, int ST, bool MASK, int ARITH>
+__global__ void __launch_bounds__(kBlockX)
+nat_fused_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::T* __restrict__ src,
+            typename Store<ST>::T* __restrict__ dst, const uint8_t* __restrict__ types) {
+    using R = typename Store<ST>::R;
+    const int x = blockIdx.x * kBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
+    const long long node = g.idx(x, y, z);
+    uint32_t L = 0;
+    if (MASK) {
+        const uint8_t t = __ldg(types + node);
+        if (t & kSolid) return;
+        L = links_of<MASK>(t, np.links, node);
+    }
+    const Nbr nb(g, x, y, z);
+    R f[Q];
+    gather_node<Q, ST, MASK>(src, g, L, nb, node, f);
+    R rho;
+    update_node<Q, ST, ARITH>(f, rho, cp);
+    store_node<Q, ST, MASK>(dst, g, np, types, L, nb, node, rho, f);
+}
+
+// FP16 storage, two x-neighbour nodes per thread (x0 even, x0 + 1).  Every
+// direction is read as one aligned half2 of the source row, so a warp moves
+// 128 B per access as the FP32 kernel does.  For c_x = +1 the pair needs
+// (x0 - 1, x0): the high half of the previous lane's pair; for c_x = -1 it
+// needs (x0 + 1, x0 + 2): the low half of the next lane's pair; lanes at a
+// warp or row edge load that one value themselves.  Rows are whole warps of
+// the same row, so neighbouring lanes hold neighbouring x.  nx must be even.
+// Arithmetic, rounding and bounce-back are those of the one-node kernel.
+//
+// Every lane in the row loads all its source rows, also when its own pair is
+// solid: its neighbours take values from it through the shuffles, and for a
+// diagonal direction those come from another row, where the node may be
+// fluid.  The loads share one guard (the lane is inside the row) so that they
+// issue together; a guard per direction splits them into separate branches
+// and measured 1.6x (D3Q19) to 2.3x (D3Q27) slower.  A source row outside a
+// walled axis only occurs for pairs in a wall row, which are solid and store
+// nothing; its address is clamped to the pair's own row.
+template <int Q, bool MASK, bool MOVING, int ARITH>
+__global__ void __launch_bounds__(kBlockX)
+nat_fused_h2_k(Geo g, CollideParams cp, NativeParams np, const __half* __restrict__ src, __half* __restrict__ dst,
+               const uint8_t* __restrict__ types) {
+    const unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int x0 = 2 * (blockIdx.x * kBlockX + threadIdx.x);
+    const int y = blockIdx.y, z = blockIdx.z;
+    const bool active = x0 < g.nx;
+    const int ym = y == 0 ? (g.wrap_y ? g.ny - 1 : y) : y - 1;
+    const int yp = y == g.ny - 1 ? (g.wrap_y ? 0 : y) : y + 1;
+    const int zm = z == 0 ? (g.wrap_z ? g.nz - 1 : z) : z - 1;
+    const int zp = z == g.nz - 1 ? (g.wrap_z ? 0 : z) : z + 1;
+    const long long yo[3] = {(long long)ym * g.ys, (long long)y * g.ys, (long long)yp * g.ys};
+    const long long zo[3] = {(long long)zm * g.zs, (long long)z * g.zs, (long long)zp * g.zs};
+    // the values the neighbouring lanes cannot provide
+    const int xm = x0 == 0 ? (g.wrap_x ? g.nx - 1 : -1) : x0 - 1;
+    const int xp2 = x0 + 2 >= g.nx ? (g.wrap_x ? x0 + 2 - g.nx : -1) : x0 + 2;
+    const bool edge_lo = lane == 0 || x0 == 0;
+    const bool edge_hi = lane == 31 || x0 + 2 >= g.nx;
+    const long long node0 = zo[1] + yo[1] + x0;
+
+    bool skip = !active;
+    uint8_t t0 = 0, t1 = 0;
+    uint32_t L0 = 0, L1 = 0;
+    if (MASK && active) {
+        const unsigned short tt = __ldg(reinterpret_cast<const unsigned short*>(types + node0));
+        t0 = (uint8_t)(tt & 0xff);
+        t1 = (uint8_t)(tt >> 8);
+        skip = (t0 & kSolid) && (t1 & kSolid);
+        L0 = links_of<MASK>(t0, np.links, node0);
+        L1 = links_of<MASK>(t1, np.links, node0 + 1);
+    }
+    float f0[Q], f1[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        const int cx = Lattice<Q>::cx(k), cy = Lattice<Q>::cy(k), cz = Lattice<Q>::cz(k);
+        const long long row = (long long)k * g.ks + zo[1 - cz] + yo[1 - cy];
+        float lo = 0.0f, hi = 0.0f;
+        if (active) {
+            const __half2 v = __ldg(reinterpret_cast<const __half2*>(src + row + x0));
+            lo = __low2float(v);
+            hi = __high2float(v);
+        }
+        if (cx == 0) {
+            f0[k] = lo;
+            f1[k] = hi;
+        } else if (cx > 0) {
+            float prev = __shfl_up_sync(kFull, hi, 1);
+            if (edge_lo) prev = (active && xm >= 0) ? __half2float(__ldg(src + row + xm)) : 0.0f;
+            f0[k] = prev;
+            f1[k] = lo;
+        } else {
+            float next = __shfl_down_sync(kFull, lo, 1);
+            if (edge_hi) next = (active && xp2 >= 0) ? __half2float(__ldg(src + row + xp2)) : 0.0f;
+            f0[k] = hi;
+            f1[k] = next;
+        }
+    }
+    if (skip) return;
+    if (MASK && (L0 | L1)) {
+#pragma unroll
+        for (int k = 1; k < Q; ++k) {
+            const long long slot = (long long)rev_of(k) * g.ks + node0;
+            if ((L0 >> rev_of(k)) & 1u) f0[k] = __half2float(__ldg(src + slot));
+            if ((L1 >> rev_of(k)) & 1u) f1[k] = __half2float(__ldg(src + slot + 1));
+        }
+    }
+    float rho0, rho1;
+    update_node<Q, 1, ARITH>(f0, rho0, cp);
+    update_node<Q, 1, ARITH>(f1, rho1, cp);
+    if (MASK && MOVING && (L0 | L1)) {
+        const Nbr n0(g, x0, y, z), n1(g, x0 + 1, y, z);
+#pragma unroll
+        for (int k = 1; k < Q; ++k) {
+            if ((L0 >> k) & 1u)
+                f0[k] = wall_corrected<Q, 1>(k, f0[k], rho0, np.vel[__ldg(types + n0.at<Q>(k, +1)) & kVelMask],
+                                             np.cs2inv);
+            if ((L1 >> k) & 1u)
+                f1[k] = wall_corrected<Q, 1>(k, f1[k], rho1, np.vel[__ldg(types + n1.at<Q>(k, +1)) & kVelMask],
+                                             np.cs2inv);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        const __half2 v = __floats2half2_rn(f0[k], f1[k]);
+        __stcs(reinterpret_cast<unsigned int*>(dst + (long long)k * g.ks + node0),
+               *reinterpret_cast<const unsigned int*>(&v));
+    }
+}
+
+// First collision from a RAW state: n at the node itself and the rho/u fields.
+template <int Q, int ST, bool MASK, int ARITH>
+__global__ void __launch_bounds__(kBlockX)
+nat_collide_raw_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::T* __restrict__ src,
+                  typename Store<ST>::T* __restrict__ dst, const float* __restrict__ rho_f,
+                  const float* __restrict__ u_f, const uint8_t* __restrict__ types) {
+    using R = typename Store<ST>::R;
+    const int x = blockIdx.x * kBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
+    const long long node = g.idx(x, y, z);
+    uint32_t L = 0;
+    if (MASK) {
+        const uint8_t t = __ldg(types + node);
+        if (t & kSolid) return;
+        L = links_of<MASK>(t, np.links, node);
+    }
+    const Nbr nb(g, x, y, z);
+    R f[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) f[k] = Store<ST>::ld(src, k * g.ks + node);
+    const R rho = (R)rho_f[node];
+    const R ux = (R)u_f[node], uy = (R)u_f[g.ks + node], uz = (R)u_f[2 * g.ks + node];
+    collide_any<Q, ST, ARITH>(f, rho, ux, uy, uz, ST == 1 ? __fsub_rn((float)rho, 1.0f) : 0.0f, cp);
+    store_node<Q, ST, MASK>(dst, g, np, types, L, nb, node, rho, f);
+}
+
+// Gather only: n (storage format) and/or moments, solid nodes reset to
+// (rho_solid, u_b) as Boundary::reset does for walls.
+template <int Q, int ST, bool MASK>
+__global__ void __launch_bounds__(kBlockX)
+nat_gather_k(Geo g, NativeParams np, const typename Store<ST>::T* __restrict__ src,
+             typename Store<ST>::T* __restrict__ n_out, float* __restrict__ rho_f,
+             float* __restrict__ u_f, const uint8_t* __restrict__ types) {
+    using R = typename Store<ST>::R;
+    const int x = blockIdx.x * kBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
+    const long long node = g.idx(x, y, z);
+    uint32_t L = 0;
+    if (MASK) {
+        const uint8_t t = __ldg(types + node);
+        if (t & kSolid) {
+            if (rho_f) {
+                const float* ub = np.vel[t & kVelMask];
+                rho_f[node] = np.rho_solid;
+                u_f[node] = ub[0]; u_f[g.ks + node] = ub[1]; u_f[2 * g.ks + node] = ub[2];
+            }
+            if (n_out) {
+                // a solid node holds no populations: they read back as 0
+#pragma unroll
+                for (int k = 0; k < Q; ++k) Store<ST>::st(n_out, k * g.ks + node, ST == 1 ? -weight<Q>(k) : (R)0);
+            }
+            return;
+        }
+        L = links_of<MASK>(t, np.links, node);
+    }
+    const Nbr nb(g, x, y, z);
+    R f[Q];
+    gather_node<Q, ST, MASK>(src, g, L, nb, node, f);
+    if (n_out) {
+#pragma unroll
+        for (int k = 0; k < Q; ++k) Store<ST>::st(n_out, k * g.ks + node, f[k]);
+    }
+    if (rho_f) {
+        R rho, ux, uy, uz;
+        moments_any<Q, ST>(f, rho, ux, uy, uz);
+        rho_f[node] = (float)rho;
+        u_f[node] = (float)ux; u_f[g.ks + node] = (float)uy; u_f[2 * g.ks + node] = (float)uz;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Batches: every domain of the batch advances one step in one launch.  The
+// work is a list of warp tasks (domain, z, i0): 32 consecutive nodes i0 ..
+// i0 + 31 of the plane z in x-fastest order, so rows shorter than a warp do
+// not leave lanes idle and a warp's loads stay within one or two rows.
+// Resident blocks take tasks round-robin.  Per node the work is that of
+// nat_fused_k: the same gather, arithmetic and bounce-back, so a domain's
+// result does not depend on which other domains share its batch.  Descriptor
+// fields are read where they are used (every lane reads the same address).
+template <int Q, int ST, int ARITH, bool MOVING>
+__global__ void __launch_bounds__(kBatchTile)
+nat_batch_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks, int ntasks, int parity) {
+    using T = typename Store<ST>::T;
+    using R = typename Store<ST>::R;
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (kBatchTile / 32);
+    for (int t = blockIdx.x * (kBatchTile / 32) + (threadIdx.x >> 5); t < ntasks; t += warps) {
+        const int4 tk = __ldg(tasks + t);
+        const BatchDomain& D = doms[tk.x];
+        const Geo g = D.g;
+        // 32 consecutive nodes of the plane z (flattened y * nx + x), so short
+        // rows do not leave lanes idle
+        const int i = tk.z + lane;
+        if (i >= g.nx * g.ny) continue;
+        const int y = (int)((unsigned)i / (unsigned)g.nx), x = i - y * g.nx, z = tk.y;
+        const long long node = g.idx(x, y, z);
+        const uint8_t* types = D.types;
+        const uint8_t tt = __ldg(types + node);
+        if (tt & kSolid) continue;
+        const NativeParams& np = D.np;
+        const uint32_t L = links_of<true>(tt, np.links, node);
+        const T* src = static_cast<const T*>(D.f[parity]);
+        T* dst = static_cast<T*>(D.f[parity ^ 1]);
+        const Nbr nb(g, x, y, z);
+        R f[Q];
+        gather_node<Q, ST, true>(src, g, L, nb, node, f);
+        R rho;
+        update_node<Q, ST, ARITH>(f, rho, D.cp);
+        store_node<Q, ST, true, MOVING>(dst, g, np, types, L, nb, node, rho, f);
+    }
+}
+
+dim3 cell_grid(const Geo& g) { return dim3((g.nx + kBlockX - 1) / kBlockX, g.ny, g.nz); }
+
+template <int Q, int ST, bool MASK, int ARITH>
+int launch_fused(const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
+                 const uint8_t* types, cudaStream_t st) {
+    using T = typename Store<ST>::T;
+    nat_fused_k<Q, ST, MASK, ARITH><<<cell_grid(g), kBlockX, 0, st>>>(g, cp, np, (const T*)src, (T*)dst, types);
+    return (int)cudaGetLastError();
+}
+
+template <int Q, int ST, bool MASK, int ARITH>
+int launch_raw(const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
+               const float* rho, const float* u, const uint8_t* types, cudaStream_t st) {
+    using T = typename Store<ST>::T;
+    nat_collide_raw_k<Q, ST, MASK, ARITH><<<cell_grid(g), kBlockX, 0, st>>>(g, cp, np, (const T*)src, (T*)dst,
+                                                                            rho, u, types);
+    return (int)cudaGetLastError();
+}
+
+template <int Q, int ST, bool MASK>
+int launch_gather(const Geo& g, const NativeParams& np, const void* src, void* n_out, float* rho, float* u,
+                  const uint8_t* types, cudaStream_t st) {
+    using T = typename Store<ST>::T;
+    nat_gather_k<Q, ST, MASK><<<cell_grid(g), kBlockX, 0, st>>>(g, np, (const T*)src, (T*)n_out, rho, u, types);
+    return (int)cudaGetLastError();
+}
+
+// ---- host-side dispatch --------------------------------------------------------
+// Calls f(ST, ARITH) (integral constants) with the kernel arithmetic of a
+// storage: FP16 and FP64 storage have one BGK arithmetic each, FP32 storage
+// plbpd's or the FP32-only one; under TRT every storage has the TRT one.
+template <int V> using IC = std::integral_constant<int, V>;
+
+template <bool TRT, class F>
+auto with_storage_arith(int storage, int arith, F&& f) {
+    if constexpr (TRT) {
+        if (storage == 1) return f(IC<1>{}, IC<kArithTRT>{});
+        if (storage == 2) return f(IC<2>{}, IC<kArithTRT>{});
+        return f(IC<0>{}, IC<kArithTRT>{});
+    } else {
+        if (storage == 1) return f(IC<1>{}, IC<kArithFP32>{});
+        if (storage == 2) return f(IC<2>{}, IC<kArithFP32>{});
+        if (arith == kArithReference) return f(IC<0>{}, IC<kArithReference>{});
+        return f(IC<0>{}, IC<kArithFP32>{});
+    }
+}
+
+template <int Q, int ARITH, bool MASK>
+int launch_fused_h2(const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
+                    const uint8_t* types, cudaStream_t st) {
+    const dim3 grid((g.nx + 2 * kBlockX - 1) / (2 * kBlockX), g.ny, g.nz);
+    if (MASK && np.moving)
+        nat_fused_h2_k<Q, true, true, ARITH><<<grid, kBlockX, 0, st>>>(g, cp, np, (const __half*)src, (__half*)dst,
+                                                                        types);
+    else
+        nat_fused_h2_k<Q, MASK, false, ARITH><<<grid, kBlockX, 0, st>>>(g, cp, np, (const __half*)src, (__half*)dst,
+                                                                         types);
+    return (int)cudaGetLastError();
+}
+
+// One fused step (FP16 storage with even nx: the pair kernel).
+template <bool TRT, int Q>
+int fused_q(int storage, int arith, bool m, const Geo& g, const CollideParams& cp, const NativeParams& np,
+            const void* src, void* dst, const uint8_t* types, cudaStream_t st) {
+    return with_storage_arith<TRT>(storage, arith, [&](auto stc, auto arc) {
+        constexpr int ST = decltype(stc)::value, AR = decltype(arc)::value;
+        if constexpr (ST == 1) {
+            if (g.nx % 2 == 0)
+                return m ? launch_fused_h2<Q, AR, true>(g, cp, np, src, dst, types, st)
+                         : launch_fused_h2<Q, AR, false>(g, cp, np, src, dst, types, st);
+        }
+        return m ? launch_fused<Q, ST, true, AR>(g, cp, np, src, dst, types, st)
+                 : launch_fused<Q, ST, false, AR>(g, cp, np, src, dst, types, st);
+    });
+}
+
+template <bool TRT, int Q>
+int raw_q(int storage, int arith, bool m, const Geo& g, const CollideParams& cp, const NativeParams& np,
+          const void* src, void* dst, const float* rho, const float* u, const uint8_t* types, cudaStream_t st) {
+    return with_storage_arith<TRT>(storage, arith, [&](auto stc, auto arc) {
+        constexpr int ST = decltype(stc)::value, AR = decltype(arc)::value;
+        return m ? launch_raw<Q, ST, true, AR>(g, cp, np, src, dst, rho, u, types, st)
+                 : launch_raw<Q, ST, false, AR>(g, cp, np, src, dst, rho, u, types, st);
+    });
+}
+
+// Batches hold FP32 or FP16 storage.
+template <bool TRT, bool MV>
+const void* batch_kernel_for(int q, int storage, int arith) {
+    if (storage == 2) return nullptr;
+    const void* k = nullptr;
+    with_storage_arith<TRT>(storage, arith, [&](auto stc, auto arc) {
+        constexpr int ST = decltype(stc)::value == 2 ? 0 : decltype(stc)::value, AR = decltype(arc)::value;
+        k = q == 9 ? (const void*)nat_batch_k<9, ST, AR, MV>
+          : q == 19 ? (const void*)nat_batch_k<19, ST, AR, MV>
+          : q == 27 ? (const void*)nat_batch_k<27, ST, AR, MV> : nullptr;
+        return 0;
+    });
+    return k;
+}
+
+template <bool TRT>
+int batch_blocks_per_sm(int q, int storage, int arith, bool moving) {
+    const void* k = moving ? batch_kernel_for<TRT, true>(q, storage, arith)
+                           : batch_kernel_for<TRT, false>(q, storage, arith);
+    if (!k) return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kBatchTile, 0) != cudaSuccess) return 0;
+    return n;
+}
+
+template <bool TRT>
+int batch_step(int q, int storage, int arith, bool moving, const BatchDomain* doms, const int4* tiles, int ntiles,
+               int parity, int blocks, cudaStream_t st) {
+    if (ntiles <= 0) return 0;
+    if (storage == 2) return (int)cudaErrorInvalidValue;
+    const int need = (ntiles + kBatchTile / 32 - 1) / (kBatchTile / 32);   // one task per warp
+    if (blocks > need) blocks = need;
+    return with_storage_arith<TRT>(storage, arith, [&](auto stc, auto arc) {
+        constexpr int ST = decltype(stc)::value == 2 ? 0 : decltype(stc)::value, AR = decltype(arc)::value;
+        auto go = [&](auto qc) {
+            constexpr int Q = decltype(qc)::value;
+            if (moving) nat_batch_k<Q, ST, AR, true><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);
+            else nat_batch_k<Q, ST, AR, false><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);
+            return (int)cudaGetLastError();
+        };
+        return q == 9 ? go(IC<9>{}) : q == 19 ? go(IC<19>{}) : q == 27 ? go(IC<27>{}) : (int)cudaErrorInvalidValue;
+    });
+}
+
+#define PLB_Q_DISPATCH(q, CALL) \
+    ((q) == 9 ? CALL(9) : (q) == 19 ? CALL(19) : (q) == 27 ? CALL(27) : (int)cudaErrorInvalidValue)
+
+}  // namespace
+}  // namespace plb

@@ -1,17 +1,26 @@
 // The solve server (plb_server_*, include/plb.h): continuous batching of
 // independent lattice-Boltzmann solves on one GPU.
 //
-// One scheduler thread owns every CUDA call.  Each loop it
+// One scheduler thread owns every CUDA call.  Running work is a set of lanes,
+// each on its own stream: a batch lane holds the small solves of one class
+// (same lattice, storage and arithmetic) and advances them as one plb_batch;
+// a solo lane holds one large solve and advances it with the solve's own
+// kernels.  Each loop the scheduler
 //   1. admits queued requests in arrival order while their device bytes fit
-//      the budget (a request larger than the whole budget fails),
-//   2. advances every class of running solves (same lattice, storage and
-//      arithmetic) by one tick -- min(tick_steps, fewest steps left in the
-//      class) -- as one batch, all classes enqueued before any is waited for,
-//   3. retires solves that have run all their steps: rho and u are copied to
-//      host memory, the solve is destroyed, its bytes return to the budget.
+//      the budget (a request larger than the whole budget fails) and routes
+//      each to a new solo lane or to its class's batch lane,
+//   2. collects the lanes whose tick has ended (an event per lane, polled):
+//      solves that have run all their steps retire -- rho and u are copied to
+//      host memory, the solve is destroyed, its bytes return to the budget,
+//   3. starts the next tick of every idle lane -- min(tick_steps, fewest
+//      steps left in the lane) -- after rebuilding a batch whose members
+//      changed,
+// so one lane's tick never waits for another's.  Device memory is
+// stream-ordered, so retiring a solve does not synchronize the device.
 // Clients submit from any thread and wait on a condition variable.
 #include <chrono>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -48,15 +57,31 @@ struct Req {
     std::string err;
 };
 
-struct Class {
+// A unit of running work with its own stream: one batch of small solves of a
+// class, or one large solve.
+struct Lane {
+    bool solo = false;
     std::vector<Req*> members;
+    std::vector<Req*> joining;     // batch lanes: admitted while a tick was in flight
     plb_batch* batch = nullptr;
-    bool dirty = true;
+    bool dirty = true;             // batch membership changed since it was built
+    cudaEvent_t done = nullptr;    // recorded after each tick
+    int64_t inflight = 0;          // steps of the tick in flight; 0 when idle
 };
 
-using ClassKey = std::tuple<int, int, int>;   // q, storage, arith
+using ClassKey = std::tuple<int, int, int, int>;   // q, storage, arith, collision
 
 long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
+
+// Solves of at least this many cells run in their own lane.
+long long solo_cells() {
+    static const long long v = [] {
+        const char* e = std::getenv("PLB_SERVER_SOLO_CELLS");
+        const long long x = e ? std::atoll(e) : 0;
+        return x > 0 ? x : (1LL << 19);
+    }();
+    return v;
+}
 
 }  // namespace
 
@@ -72,7 +97,9 @@ struct plb_server {
     std::deque<Req*> pending;
     std::unordered_map<int64_t, std::unique_ptr<Req>> reqs;
     int64_t next_id = 1;
-    std::map<ClassKey, Class> classes;   // scheduler thread only
+    // scheduler thread only
+    std::map<ClassKey, std::unique_ptr<Lane>> batch_lanes;
+    std::vector<std::unique_ptr<Lane>> solo_lanes;
 
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 };
@@ -121,16 +148,86 @@ void retire(plb_server* srv, Req* r) {
     finish(srv, r, err.empty() ? PLB_REQ_DONE : PLB_REQ_FAILED, err);
 }
 
+void fail_lane(plb_server* srv, Lane& L, const std::string& e) {
+    if (L.batch) plb_batch_destroy(L.batch);
+    L.batch = nullptr;
+    for (std::vector<Req*>* v : {&L.members, &L.joining})
+        for (Req* r : *v) {
+            if (r->s) plb_solve_destroy(r->s);
+            r->s = nullptr;
+            finish(srv, r, PLB_REQ_FAILED, e);
+        }
+    L.members.clear();
+    L.joining.clear();
+    L.inflight = 0;
+    L.dirty = true;
+}
+
+// Starts the next tick of an idle lane with members.
+void launch_tick(plb_server* srv, Lane& L) {
+    if (!L.done && cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming) != cudaSuccess) {
+        fail_lane(srv, L, "cudaEventCreate failed");
+        return;
+    }
+    int64_t t = srv->tick;
+    for (Req* r : L.members) t = r->remaining < t ? r->remaining : t;
+    if (t < 1) t = 1;
+    void* stream = nullptr;
+    if (L.solo) {
+        if (plb_step_async(L.members[0]->s, t) != PLB_OK) return fail_lane(srv, L, plb_last_error());
+        stream = plb_stream_handle(L.members[0]->s);
+    } else {
+        if (L.dirty) {
+            if (L.batch) plb_batch_destroy(L.batch);
+            L.batch = nullptr;
+            std::vector<plb_solve*> ss;
+            for (Req* r : L.members) ss.push_back(r->s);
+            if (plb_batch_create((int32_t)ss.size(), ss.data(), &L.batch) != PLB_OK)
+                return fail_lane(srv, L, plb_last_error());
+            L.dirty = false;
+        }
+        if (plb_batch_step_async(L.batch, t) != PLB_OK) return fail_lane(srv, L, plb_last_error());
+        stream = plb_batch_stream_handle(L.batch);
+    }
+    if (cudaEventRecord(L.done, (cudaStream_t)stream) != cudaSuccess) return fail_lane(srv, L, "cudaEventRecord failed");
+    L.inflight = t;
+}
+
+// Collects a lane whose tick has ended; returns false while it still runs.
+bool collect_tick(plb_server* srv, Lane& L) {
+    const cudaError_t q = cudaEventQuery(L.done);
+    if (q == cudaErrorNotReady) return false;
+    if (q != cudaSuccess) {
+        fail_lane(srv, L, std::string("tick failed: ") + cudaGetErrorString(q));
+        return true;
+    }
+    std::vector<Req*> keep;
+    for (Req* r : L.members) {
+        r->remaining -= L.inflight;
+        if (r->remaining <= 0) {
+            retire(srv, r);
+            L.dirty = true;
+        } else {
+            keep.push_back(r);
+        }
+    }
+    L.members.swap(keep);
+    L.inflight = 0;
+    return true;
+}
+
 void scheduler(plb_server* srv) {
     cudaSetDevice(srv->device);
     for (;;) {
         // 1. admission
         std::vector<Req*> admitted;
+        size_t waiting = 0;   // requests left queued (no room yet)
         {
             std::unique_lock<std::mutex> lk(srv->mu);
-            bool running = false;
-            for (auto& kv : srv->classes) running |= !kv.second.members.empty();
-            if (!running)
+            bool busy = !srv->solo_lanes.empty();
+            for (auto& kv : srv->batch_lanes)
+                busy |= !kv.second->members.empty() || !kv.second->joining.empty();
+            if (!busy)
                 srv->work_cv.wait(lk, [&] { return srv->stop || !srv->pending.empty(); });
             if (srv->stop) break;
             while (!srv->pending.empty()) {
@@ -153,6 +250,7 @@ void scheduler(plb_server* srv) {
                 r->t_adm = srv->now();
                 admitted.push_back(r);
             }
+            waiting = srv->pending.size();
         }
         for (Req* r : admitted) {
             const std::string e = start_solve(r);
@@ -160,77 +258,65 @@ void scheduler(plb_server* srv) {
                 finish(srv, r, PLB_REQ_FAILED, e);
                 continue;
             }
-            Class& c = srv->classes[ClassKey(r->p.q, r->p.storage, r->p.arith)];
-            c.members.push_back(r);
-            c.dirty = true;
+            if (r->p.nx * r->p.ny * r->p.nz >= solo_cells()) {
+                auto L = std::make_unique<Lane>();
+                L->solo = true;
+                L->members.push_back(r);
+                srv->solo_lanes.push_back(std::move(L));
+            } else {
+                auto& L = srv->batch_lanes[ClassKey(r->p.q, r->p.storage, r->p.arith, r->p.collision)];
+                if (!L) L = std::make_unique<Lane>();
+                L->joining.push_back(r);
+            }
         }
-        // 2. one tick for every class
-        std::vector<std::pair<Class*, int64_t>> ticking;
-        for (auto& kv : srv->classes) {
-            Class& c = kv.second;
-            if (c.members.empty()) continue;
-            if (c.dirty) {
-                if (c.batch) plb_batch_destroy(c.batch);
-                c.batch = nullptr;
-                std::vector<plb_solve*> ss;
-                for (Req* r : c.members) ss.push_back(r->s);
-                if (plb_batch_create((int32_t)ss.size(), ss.data(), &c.batch) != PLB_OK) {
-                    const std::string e = plb_last_error();
-                    for (Req* r : c.members) {
-                        plb_solve_destroy(r->s);
-                        r->s = nullptr;
-                        finish(srv, r, PLB_REQ_FAILED, e);
-                    }
-                    c.members.clear();
-                    continue;
-                }
-                c.dirty = false;
+        // 2. collect ended ticks, 3. start the next ones
+        bool progressed = !admitted.empty();
+        auto service = [&](Lane& L) {
+            if (L.inflight && !collect_tick(srv, L)) return;
+            if (!L.joining.empty()) {
+                L.members.insert(L.members.end(), L.joining.begin(), L.joining.end());
+                L.joining.clear();
+                L.dirty = true;
             }
-            int64_t t = srv->tick;
-            for (Req* r : c.members) t = r->remaining < t ? r->remaining : t;
-            if (t < 1) t = 1;
-            if (plb_batch_step_async(c.batch, t) != PLB_OK) {
-                const std::string e = plb_last_error();
-                for (Req* r : c.members) {
-                    plb_solve_destroy(r->s);
-                    r->s = nullptr;
-                    finish(srv, r, PLB_REQ_FAILED, e);
-                }
-                c.members.clear();
-                plb_batch_destroy(c.batch);
-                c.batch = nullptr;
-                continue;
+            if (L.members.empty()) {
+                if (L.batch) plb_batch_destroy(L.batch);
+                L.batch = nullptr;
+                return;
             }
-            ticking.emplace_back(&c, t);
+            launch_tick(srv, L);
+            progressed = true;
+        };
+        for (auto& kv : srv->batch_lanes) service(*kv.second);
+        for (auto& L : srv->solo_lanes) service(*L);
+        for (size_t i = 0; i < srv->solo_lanes.size();) {
+            Lane& L = *srv->solo_lanes[i];
+            if (L.members.empty() && !L.inflight) {
+                if (L.done) cudaEventDestroy(L.done);
+                srv->solo_lanes.erase(srv->solo_lanes.begin() + (long)i);
+            } else {
+                ++i;
+            }
         }
-        // 3. retire
-        for (auto& ct : ticking) {
-            Class& c = *ct.first;
-            plb_batch_synchronize(c.batch);
-            std::vector<Req*> keep;
-            for (Req* r : c.members) {
-                r->remaining -= ct.second;
-                if (r->remaining <= 0) {
-                    retire(srv, r);
-                    c.dirty = true;
-                } else {
-                    keep.push_back(r);
-                }
-            }
-            c.members.swap(keep);
-            if (c.members.empty() && c.batch) {
-                plb_batch_destroy(c.batch);
-                c.batch = nullptr;
-            }
+        if (!progressed) {
+            // every lane is mid-tick: sleep briefly, or until a new request arrives
+            std::unique_lock<std::mutex> lk(srv->mu);
+            srv->work_cv.wait_for(lk, std::chrono::microseconds(200),
+                                  [&] { return srv->stop || srv->pending.size() > waiting; });
         }
     }
-    // stop: drop everything
-    for (auto& kv : srv->classes) {
-        if (kv.second.batch) plb_batch_destroy(kv.second.batch);
-        for (Req* r : kv.second.members)
-            if (r->s) plb_solve_destroy(r->s);
-    }
-    srv->classes.clear();
+    // stop: wait for the ticks in flight, then drop everything
+    auto drop = [&](Lane& L) {
+        if (L.inflight) cudaEventSynchronize(L.done);
+        if (L.batch) plb_batch_destroy(L.batch);
+        for (std::vector<Req*>* v : {&L.members, &L.joining})
+            for (Req* r : *v)
+                if (r->s) plb_solve_destroy(r->s);
+        if (L.done) cudaEventDestroy(L.done);
+    };
+    for (auto& kv : srv->batch_lanes) drop(*kv.second);
+    for (auto& L : srv->solo_lanes) drop(*L);
+    srv->batch_lanes.clear();
+    srv->solo_lanes.clear();
 }
 
 }  // namespace
