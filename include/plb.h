@@ -74,16 +74,21 @@ extern "C" {
 
 /* Population storage.  FP16_DEV keeps f_k - w_k in IEEE half precision and
  * does all collision arithmetic in FP32 (NATIVE semantics only).  FP64
- * keeps populations and arithmetic in double: the reference run that
- * reduced-precision runs are measured against (NATIVE semantics only).    */
+ * keeps populations and arithmetic in double with the exact weights: the
+ * reference run that reduced-precision runs are measured against (NATIVE
+ * semantics only).  FP32_DEV keeps f_k - w_k in FP32 with FP16_DEV's
+ * arithmetic: FP32's bytes, with the precision kept in the small deviation
+ * that carries the flow (NATIVE semantics only).                          */
 #define PLB_STORAGE_FP32 0
 #define PLB_STORAGE_FP16_DEV 1
 #define PLB_STORAGE_FP64 2
+#define PLB_STORAGE_FP32_DEV 3
 
 /* Collision operator.  BGK is plbpd's CollisionSRT (src/CollisionSRT.cpp),
  * body force as the velocity shift u + F tau/rho.  TRT is an extension
- * through plbpd's Collision base (src/Collision.hpp:10-21), NATIVE semantics
- * only, with PLB_ARITH_FP32 or FP16/FP64 storage: the even part of each pair
+ * through plbpd's Collision base (src/Collision.hpp:10-21), under either
+ * semantics, always in FP32 arithmetic (FP64 with FP64 storage; `arith` is
+ * not used): the even part of each pair
  * of opposite directions relaxes with 1/tau, the odd part with 1/tau_m,
  * tau_m = trt_magic/(tau - 1/2) + 1/2 (trt_magic 0 selects 3/16, which puts
  * the half-way bounce-back wall exactly half way), and the force enters as a
@@ -91,6 +96,16 @@ extern "C" {
  * is sum(c_k f_k)/rho under both operators, as plbpd's CalcMoments reports it. */
 #define PLB_COLLISION_BGK 0
 #define PLB_COLLISION_TRT 1
+
+/* Streaming (NATIVE semantics).  AB: two population buffers, each step
+ * reads one and writes the other.  AA: one buffer updated in place,
+ * alternating a step that touches only the node's own slots with one that
+ * reads and writes the neighbours' (the reference's Streaming leaves its
+ * pull variant unimplemented, src/Streaming.cpp:96-102): half the device
+ * memory, the same bytes per step, bit-identical results.  Batches take AB
+ * solves only. */
+#define PLB_STREAMING_AB 0
+#define PLB_STREAMING_AA 1
 
 /* Field ids: plbpd's SimData members n, ntmp, rho, u (src/SimData.hpp:18-21). */
 #define PLB_FIELD_N 0
@@ -122,6 +137,7 @@ typedef struct plb_params {
     int32_t device;             /* CUDA device ordinal                              */
     int32_t collision;          /* PLB_COLLISION_* (0: BGK)                         */
     float trt_magic;            /* TRT: (tau - 1/2)(tau_m - 1/2); 0 selects 3/16    */
+    int32_t streaming;          /* PLB_STREAMING_* (0: AB)                          */
 } plb_params;
 
 /* ---- library ----------------------------------------------------------- */
@@ -159,6 +175,10 @@ int plb_set_relaxation(plb_solve* s, float nu, const float* force3);
 /* Replace the boundary description of an existing solve (REFERENCE
  * semantics), as constructing another Boundary (src/Boundary.cpp:20-32) and
  * applying it to the same SimData would.  Arguments as in plb_params. */
+/* Switches the collision operator (PLB_COLLISION_*, with the TRT magic
+ * parameter) of an existing solve; the façade's CollisionTRT uses it.  No
+ * counterpart in plbpd, whose LBDynamics constructs its CollisionSRT. */
+int plb_set_collision(plb_solve* s, int32_t collision, float trt_magic);
 int plb_set_boundary(plb_solve* s, float rho_solid, const int32_t* face_type6, const int32_t* face_has_vel6,
                      const float* face_vel18);
 

@@ -56,6 +56,11 @@ static const int32_t kD3Q27[27][3] = {
     {1, 1, 1}, {-1, -1, -1}, {1, 1, -1}, {-1, -1, 1}, {1, -1, 1}, {-1, 1, -1},
     {-1, 1, 1}, {1, -1, -1}};
 
+/* Populations held as deviations d = f - w (float instantiation). */
+static int orc_dev(const orc_sim* s) {
+    return !s->precision && (s->arith == ORC_ARITH_FP16DEV || s->arith == ORC_ARITH_FP32DEV);
+}
+
 /* Weight of a velocity with |c|^2 = sp, as the reference's double literal. */
 static double weight_exact(int q, int sp) {
     if (q == 9) return sp == 0 ? 4. / 9. : (sp == 1 ? 1. / 9. : 1. / 36.);
@@ -270,8 +275,8 @@ void orc_destroy(orc_sim* s) {
 }
 
 int orc_set_trt(orc_sim* s, float magic) {
-    if (s->mode != ORC_MODE_NATIVE || !(s->tau > 0.5f)) return -1;
-    if (s->precision == 0 && s->arith != ORC_ARITH_FP32 && s->arith != ORC_ARITH_FP16DEV) return -1;
+    if (!(s->tau > 0.5f)) return -1;
+    if (s->precision == 0 && s->arith != ORC_ARITH_FP32 && !orc_dev(s)) return -1;
     const double lam = magic > 0.0f ? (double)magic : 3.0 / 16.0;
     const double tau_m = lam / ((double)s->tau - 0.5) + 0.5;
     s->trt = 1;
@@ -342,14 +347,14 @@ static void* orc_field_ptr(const orc_sim* s, int which) {
     }
 }
 
-static int orc_fp16_pop(const orc_sim* s, int which) {
-    return !s->precision && s->arith == ORC_ARITH_FP16DEV && (which == ORC_N || which == ORC_NTMP);
+static int orc_dev_pop(const orc_sim* s, int which) {
+    return !s->precision && orc_dev(s) && (which == ORC_N || which == ORC_NTMP);
 }
 
 void orc_get_field(const orc_sim* s, int which, float* out) {
     const size_t len = orc_field_len(s, which);
     const void* p = orc_field_ptr(s, which);
-    if (orc_fp16_pop(s, which)) {   /* populations are w + d */
+    if (orc_dev_pop(s, which)) {   /* populations are w + d */
         const float* d = (const float*)p;
         for (size_t i = 0; i < len; ++i) out[i] = d[i] + s->w[i % (size_t)s->q];
         return;
@@ -365,9 +370,12 @@ void orc_get_field(const orc_sim* s, int which, float* out) {
 void orc_set_field(orc_sim* s, int which, const float* in) {
     const size_t len = orc_field_len(s, which);
     void* p = orc_field_ptr(s, which);
-    if (orc_fp16_pop(s, which)) {
+    if (orc_dev_pop(s, which)) {
         float* d = (float*)p;
-        for (size_t i = 0; i < len; ++i) d[i] = orc_round_half(in[i] - s->w[i % (size_t)s->q]);
+        for (size_t i = 0; i < len; ++i) {
+            const float v = in[i] - s->w[i % (size_t)s->q];
+            d[i] = s->arith == ORC_ARITH_FP16DEV ? orc_round_half(v) : v;
+        }
         return;
     }
     if (!s->precision && which == ORC_RHO)

@@ -49,7 +49,10 @@ enum { ORC_ARITH_AVX2 = 0, ORC_ARITH_SCALAR = 1, ORC_ARITH_FP32 = 2,
         * FP32 in deviation form (the engine's FP16 storage):
         *   drho = sum d_k, rho = 1 + drho, u = (sum c_k d_k) / rho,
         *   d'_k = (1-omega) d_k + omega w_k (drho + rho (3cu + 4.5cu^2 - 1.5usq)) */
-       ORC_ARITH_FP16DEV = 3 };
+       ORC_ARITH_FP16DEV = 3,
+       /* the same deviation form with d kept in FP32, not rounded to binary16
+        * (the engine's FP32 deviation storage) */
+       ORC_ARITH_FP32DEV = 4 };
 enum { ORC_FACE_NONE = 0, ORC_FACE_PERIODIC = 1, ORC_FACE_NOSLIP = 2 };
 /* field ids */
 enum { ORC_N = 0, ORC_NTMP = 1, ORC_RHO = 2, ORC_U = 3 };
@@ -75,8 +78,8 @@ void orc_destroy(orc_sim* s);
 void orc_set_threads(int n);
 int orc_max_threads(void);
 
-/* Two-relaxation-time collision for ORC_MODE_NATIVE (float arithmetic
- * ORC_ARITH_FP32 or ORC_ARITH_FP16DEV, or double precision).  The even part
+/* Two-relaxation-time collision (float arithmetic ORC_ARITH_FP32 or a
+ * deviation form, or double precision), in either mode.  The even part
  * of each pair (k, r = rev k) relaxes with omega = 1/tau, the odd part with
  * omega_m = 1/tau_m, tau_m = magic/(tau - 1/2) + 1/2 (magic 0 selects 3/16),
  * and the body force enters as a second-order source (no velocity shift):
@@ -86,8 +89,8 @@ int orc_max_threads(void);
  *   f_k' = f_k - omega (f+ - e+) - omega_m (f- - e-) + S+ + S-,
  *   f_r' = f_r - omega (f+ - e+) + omega_m (f- - e-) + S+ - S-.
  * With magic 3/16 and half-way bounce-back, plane Poiseuille flow is exact.
- * Returns 0, or -1 when the mode, arithmetic or tau (must exceed 1/2) does
- * not allow it. */
+ * Returns 0, or -1 when the arithmetic or tau (must exceed 1/2) does not
+ * allow it. */
 int orc_set_trt(orc_sim* s, float magic);
 
 /* Obstacle mask for ORC_MODE_NATIVE: nz*ny*nx bytes (x fastest), nonzero = solid. */

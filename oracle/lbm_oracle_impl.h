@@ -73,7 +73,7 @@ static void FN(collide_node)(const orc_sim* s, R* nl, R rho, const R* ul, R drho
     if (s->trt) {
         /* TRT with a second-order force source; pairs (k, k + 1), k odd.
          * FP16DEV works on deviations d = f - w: e+ - w = w (drho + rho (4.5cu^2 - 1.5usq)) */
-        const int dev = s->arith == ORC_ARITH_FP16DEV;
+        const int dev = orc_dev(s);
         const float omm = s->omega_m;
         const float gp = 1.0f - 0.5f * omega, gm = 1.0f - 0.5f * omm;
         const float hr = 0.5f / rho;
@@ -104,7 +104,7 @@ static void FN(collide_node)(const orc_sim* s, R* nl, R rho, const R* ul, R drho
         }
         return;
     }
-    if (s->arith == ORC_ARITH_FP16DEV) {
+    if (orc_dev(s)) {
         /* deviation form: nl holds d = f - w;
          * X = 3cu + 4.5cu^2 - 1.5usq, d' = (1-omega) d + w (omega rho X + omega drho) */
         const float kusq16 = -1.5f * usq;
@@ -345,7 +345,7 @@ static void FN(moments)(orc_sim* s) {
                     uz += nk * (R)s->c[k][2];
                 }
 #if !ORC_IS_DOUBLE
-                if (s->arith == ORC_ARITH_FP16DEV) {   /* r is the density deviation */
+                if (orc_dev(s)) {   /* r is the density deviation */
                     s->drho[i] = r;
                     r = 1.0f + r;
                 }
@@ -419,8 +419,11 @@ static void FN(init_fields)(orc_sim* s) {
     }
 #else
     orc_eqlb(s->q, s->rho0, s->u0, feq);
-    if (s->arith == ORC_ARITH_FP16DEV)
-        for (int k = 0; k < s->q; ++k) feq[k] = orc_round_half(feq[k] - s->w[k]);
+    if (orc_dev(s))
+        for (int k = 0; k < s->q; ++k) {
+            feq[k] = feq[k] - s->w[k];
+            if (s->arith == ORC_ARITH_FP16DEV) feq[k] = orc_round_half(feq[k]);
+        }
 #endif
     for (size_t i = 0; i < cells; ++i) {
         s->drho[i] = s->rho0 - 1.0f;
@@ -443,7 +446,7 @@ static void FN(conservation)(const orc_sim* s, double* out) {
                 if (s->solid[i]) continue;
                 for (int k = 0; k < s->q; ++k) {
                     double v = (double)n[i * s->q + k];
-                    if (s->arith == ORC_ARITH_FP16DEV && !ORC_IS_DOUBLE) v += (double)s->w[k];
+                    if (orc_dev(s) && !ORC_IS_DOUBLE) v += (double)s->w[k];
                     m += v;
                     px += v * s->c[k][0];
                     py += v * s->c[k][1];

@@ -27,7 +27,7 @@ REF_DIR = os.path.join(HERE, "_ref")
 FACES = ("east", "west", "north", "south", "up", "down")
 FACE_NONE, FACE_PERIODIC, FACE_NOSLIP = 0, 1, 2
 MODE_REFERENCE, MODE_NATIVE = 0, 1
-ARITH_AVX2, ARITH_SCALAR, ARITH_FP32, ARITH_FP16DEV = 0, 1, 2, 3
+ARITH_AVX2, ARITH_SCALAR, ARITH_FP32, ARITH_FP16DEV, ARITH_FP32DEV = 0, 1, 2, 3, 4
 N, NTMP, RHO, U = 0, 1, 2, 3
 Q_OF = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27}
 
@@ -131,7 +131,7 @@ class Port(_Sim):
                 raise ValueError("mask needs MODE_NATIVE")
         if trt is not None:   # the TRT magic parameter (0 selects 3/16)
             if self.lib.orc_set_trt(self.h, float(trt)) != 0:
-                raise ValueError("TRT needs MODE_NATIVE, FP32/FP16DEV arithmetic or double, and tau > 1/2")
+                raise ValueError("TRT needs FP32/FP16DEV arithmetic or double, and tau > 1/2")
 
     def __del__(self):
         h = getattr(self, "h", None)

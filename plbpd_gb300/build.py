@@ -24,8 +24,9 @@ LIB = os.path.join(OUT, "libplb_gb300.so")
 SOURCES = ["capi.cu", "kernels_ref.cu", "kernels_native.cu", "kernels_trt.cu", "kernels_util.cu", "kernels_static.cu",
            "facade.cpp", "server.cpp"]
 HEADERS = ["lattice.cuh", "engine.h", "native_impl.cuh"]
-FACADE_HEADERS = ["Boundary.hpp", "CalcMoments.hpp", "Collision.hpp", "CollisionSRT.hpp", "Domain.hpp", "EqlbDist.hpp",
-                  "Field.hpp", "Flow.hpp", "LBDynamics.hpp", "LBModel.hpp", "PLBPD.hpp", "SimData.hpp", "Streaming.hpp"]
+FACADE_HEADERS = ["Boundary.hpp", "CalcMoments.hpp", "Collision.hpp", "CollisionSRT.hpp", "CollisionTRT.hpp", "Domain.hpp",
+                  "EqlbDist.hpp", "Field.hpp", "Flow.hpp", "LBDynamics.hpp", "LBModel.hpp", "PLBPD.hpp", "SimData.hpp",
+                  "Streaming.hpp"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",

@@ -20,7 +20,8 @@ FACES = ("east", "west", "north", "south", "up", "down")
 SEMANTICS_REFERENCE, SEMANTICS_NATIVE = 0, 1
 ARITH_REFERENCE, ARITH_FP32 = 0, 1
 COLLISION_BGK, COLLISION_TRT = 0, 1
-STORAGE_FP32, STORAGE_FP16_DEV, STORAGE_FP64 = 0, 1, 2
+STREAMING_AB, STREAMING_AA = 0, 1
+STORAGE_FP32, STORAGE_FP16_DEV, STORAGE_FP64, STORAGE_FP32_DEV = 0, 1, 2, 3
 FIELD_N, FIELD_NTMP, FIELD_RHO, FIELD_U = 0, 1, 2, 3
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 Q_OF = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27}
@@ -37,7 +38,8 @@ class Params(C.Structure):
                 ("nu", C.c_float), ("rho0", C.c_float), ("u0", C.c_float * 3), ("force", C.c_float * 3),
                 ("rho_solid", C.c_float), ("face_type", C.c_int32 * 6), ("face_has_vel", C.c_int32 * 6),
                 ("face_vel", (C.c_float * 3) * 6), ("semantics", C.c_int32), ("arith", C.c_int32),
-                ("storage", C.c_int32), ("device", C.c_int32), ("collision", C.c_int32), ("trt_magic", C.c_float)]
+                ("storage", C.c_int32), ("device", C.c_int32), ("collision", C.c_int32), ("trt_magic", C.c_float),
+                ("streaming", C.c_int32)]
 
 
 # (name, restype, argtypes) of every entry point declared in include/plb.h
@@ -50,6 +52,7 @@ _SIGS = [
     ("plb_solve_create", C.c_int, [C.POINTER(Params), C.POINTER(C.c_void_p)]),
     ("plb_solve_destroy", C.c_int, [C.c_void_p]),
     ("plb_set_relaxation", C.c_int, [C.c_void_p, C.c_float, C.c_void_p]),
+    ("plb_set_collision", C.c_int, [C.c_void_p, C.c_int32, C.c_float]),
     ("plb_set_boundary", C.c_int, [C.c_void_p, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("plb_set_mask", C.c_int, [C.c_void_p, C.c_void_p]),
     ("plb_initialize", C.c_int, [C.c_void_p]),
@@ -148,7 +151,7 @@ def make_params(model: str, nx: int, ny: int, nz: int, nu: float, rho0: float = 
                 force=(0, 0, 0), rho_solid: float = 1.0, face_type: dict | None = None,
                 face_vel: dict | None = None, semantics: int = SEMANTICS_REFERENCE,
                 arith: int = ARITH_REFERENCE, storage: int = STORAGE_FP32, device: int = 0,
-                collision: int = COLLISION_BGK, trt_magic: float = 0.0) -> Params:
+                collision: int = COLLISION_BGK, trt_magic: float = 0.0, streaming: int = STREAMING_AB) -> Params:
     face_type = face_type or {}
     face_vel = face_vel or {}
     p = Params()
@@ -166,7 +169,7 @@ def make_params(model: str, nx: int, ny: int, nz: int, nu: float, rho0: float = 
             for i in range(3):
                 p.face_vel[f][i] = float(face_vel[name][i])
     p.semantics, p.arith, p.storage, p.device = int(semantics), int(arith), int(storage), int(device)
-    p.collision, p.trt_magic = int(collision), float(trt_magic)
+    p.collision, p.trt_magic, p.streaming = int(collision), float(trt_magic), int(streaming)
     return p
 
 
@@ -213,6 +216,9 @@ class Solve:
         m = np.ascontiguousarray(mask, dtype=np.uint8)
         assert m.shape == (self.nz, self.ny, self.nx)
         check(lib().plb_set_mask(self.h, _ptr(m)))
+
+    def set_collision(self, collision: int, trt_magic: float = 0.0) -> None:
+        check(lib().plb_set_collision(self.h, int(collision), float(trt_magic)))
 
     def initialize(self) -> None: check(lib().plb_initialize(self.h))
     def step(self, n: int = 1) -> None: check(lib().plb_step(self.h, int(n)))

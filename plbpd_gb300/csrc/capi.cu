@@ -128,6 +128,10 @@ struct plb_solve {
     bool fields_valid = true;
     // NATIVE: false = RAW (buffer cur holds n), true = POST (holds P_{t-1})
     bool post = false;
+    // NATIVE AA streaming: one buffer f[0]; `swapped` after an even step
+    // (A[rev k][x] = n*_k(x)), natural after an odd one (A[k][x] = n_k(x))
+    bool aa = false;
+    bool swapped = false;
     // no-slip launch groups (REFERENCE)
     int groups[6][2];
     int group_len[6];
@@ -138,6 +142,13 @@ struct plb_solve {
 };
 
 namespace {
+
+size_t esize_of(int storage) {
+    return storage == PLB_STORAGE_FP16_DEV ? 2 : storage == PLB_STORAGE_FP64 ? 8 : 4;
+}
+
+// Bytes of one population buffer.
+size_t pop_bytes(const plb_solve* s) { return (size_t)s->q * (size_t)s->g.ks * esize_of(s->storage); }
 
 int set_device(const plb_solve* s) {
     int cur = -1;
@@ -272,16 +283,18 @@ int validate(const plb_params* p) {
     if (p->semantics != PLB_SEMANTICS_REFERENCE && p->semantics != PLB_SEMANTICS_NATIVE)
         return fail(PLB_EINVAL, "invalid semantics");
     if (p->arith != PLB_ARITH_REFERENCE && p->arith != PLB_ARITH_FP32) return fail(PLB_EINVAL, "invalid arith");
-    if (p->storage != PLB_STORAGE_FP32 && p->storage != PLB_STORAGE_FP16_DEV && p->storage != PLB_STORAGE_FP64)
+    if (p->storage != PLB_STORAGE_FP32 && p->storage != PLB_STORAGE_FP16_DEV && p->storage != PLB_STORAGE_FP64 &&
+        p->storage != PLB_STORAGE_FP32_DEV)
         return fail(PLB_EINVAL, "invalid storage");
     if (p->storage != PLB_STORAGE_FP32 && p->semantics != PLB_SEMANTICS_NATIVE)
-        return fail(PLB_EUNSUPPORTED, "FP16 and FP64 storage need NATIVE semantics");
+        return fail(PLB_EUNSUPPORTED, "FP16, FP64 and FP32 deviation storage need NATIVE semantics");
     if (p->collision != PLB_COLLISION_BGK && p->collision != PLB_COLLISION_TRT)
         return fail(PLB_EINVAL, "invalid collision operator");
+    if (p->streaming != PLB_STREAMING_AB && p->streaming != PLB_STREAMING_AA)
+        return fail(PLB_EINVAL, "invalid streaming");
+    if (p->streaming == PLB_STREAMING_AA && p->semantics != PLB_SEMANTICS_NATIVE)
+        return fail(PLB_EUNSUPPORTED, "AA streaming needs NATIVE semantics");
     if (p->collision == PLB_COLLISION_TRT) {
-        if (p->semantics != PLB_SEMANTICS_NATIVE) return fail(PLB_EUNSUPPORTED, "TRT needs NATIVE semantics");
-        if (p->storage == PLB_STORAGE_FP32 && p->arith != PLB_ARITH_FP32)
-            return fail(PLB_EUNSUPPORTED, "TRT with FP32 storage needs PLB_ARITH_FP32");
         if (!(p->trt_magic >= 0.0f) || p->trt_magic > 1e30f) return fail(PLB_EINVAL, "invalid TRT magic parameter");
         if (!(3.0f * p->nu + 0.5f > 0.5f)) return fail(PLB_EINVAL, "TRT needs tau > 1/2 (nu > 0)");
     }
@@ -341,7 +354,7 @@ int ref_boundary(plb_solve* s) {
 }
 
 int ref_one_step(plb_solve* s, bool first, bool wb_all) {
-    PLB_KERNEL(ref_fused_step(s->q, s->p.arith, first, wb_all, s->g, s->cp, s->fp, (float*)s->f[s->cur],
+    PLB_KERNEL(ref_fused_step(s->q, s->karith, first, wb_all, s->g, s->cp, s->fp, (float*)s->f[s->cur],
                               (float*)s->f[1 - s->cur], s->rho, s->u, s->stream));
     s->cur = 1 - s->cur;
     return ref_boundary(s);
@@ -359,6 +372,12 @@ int ref_materialize_fields(plb_solve* s) {
 
 // ---- NATIVE semantics ------------------------------------------------------
 int nat_one_step(plb_solve* s) {
+    if (s->aa) {
+        PLB_KERNEL(nat_aa_step(s->swapped ? 2 : 1, s->q, s->storage, s->karith, s->has_mask, s->g, s->cp, s->np,
+                               s->f[0], s->rho, s->u, s->types, s->stream));
+        s->swapped = !s->swapped;
+        return PLB_OK;
+    }
     PLB_KERNEL(nat_fused_step(s->q, s->storage, s->karith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
                               s->f[1 - s->cur], s->types, s->stream));
     s->cur = 1 - s->cur;
@@ -378,6 +397,28 @@ int nat_gather_to_other(plb_solve* s) {
 // replaces part of it).
 int nat_materialize(plb_solve* s) {
     if (!s->post) return PLB_OK;
+    if (s->aa) {
+        if (s->swapped) {
+            // the natural layout cannot be rebuilt in place: gather into a
+            // transient buffer and copy it back
+            const size_t bytes = pop_bytes(s);
+            void* tmp = nullptr;
+            PLB_CUDA(cudaMallocAsync(&tmp, bytes, s->stream));
+            const int e = nat_aa_gather(s->q, s->storage, s->has_mask, true, s->g, s->np, s->f[0], tmp, s->rho, s->u,
+                                        s->types, s->stream);
+            const cudaError_t c = e == 0 ? cudaMemcpyAsync(s->f[0], tmp, bytes, cudaMemcpyDeviceToDevice, s->stream)
+                                         : cudaSuccess;
+            cudaFreeAsync(tmp, s->stream);
+            if (e != 0) return fail(PLB_ECUDA, std::string("nat_aa_gather: ") + cudaGetErrorString((cudaError_t)e));
+            if (c != cudaSuccess) return fail(PLB_ECUDA, std::string("cudaMemcpyAsync: ") + cudaGetErrorString(c));
+        } else {
+            PLB_KERNEL(nat_aa_gather(s->q, s->storage, s->has_mask, false, s->g, s->np, s->f[0], nullptr, s->rho,
+                                     s->u, s->types, s->stream));
+        }
+        s->post = false;
+        s->swapped = false;
+        return PLB_OK;
+    }
     PLB_TRY(nat_gather_to_other(s));
     s->cur = 1 - s->cur;
     s->post = false;
@@ -401,7 +442,8 @@ int capture_chunk(plb_solve* s, int parity) {
 }
 
 int run_chunk(plb_solve* s) {
-    const int parity = s->cur;
+    // a chunk has an even number of steps, so it ends in the state it began
+    const int parity = s->aa ? (int)s->swapped : s->cur;
     if (!s->graph[parity]) {
         PLB_TRY(capture_chunk(s, parity));   // capture toggles cur an even number of times
     }
@@ -427,9 +469,15 @@ int march(plb_solve* s, int64_t n) {
     }
     int64_t done = 0;
     if (!s->post) {
-        PLB_KERNEL(nat_collide_raw(s->q, s->storage, s->karith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
-                                   s->f[1 - s->cur], s->rho, s->u, s->types, s->stream));
-        s->cur = 1 - s->cur;
+        if (s->aa) {
+            PLB_KERNEL(nat_aa_step(0, s->q, s->storage, s->karith, s->has_mask, s->g, s->cp, s->np, s->f[0], s->rho,
+                                   s->u, s->types, s->stream));
+            s->swapped = true;
+        } else {
+            PLB_KERNEL(nat_collide_raw(s->q, s->storage, s->karith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
+                                       s->f[1 - s->cur], s->rho, s->u, s->types, s->stream));
+            s->cur = 1 - s->cur;
+        }
         s->post = true;
         done = 1;
     }
@@ -486,6 +534,7 @@ int plb_solve_create(const plb_params* params, plb_solve** out) {
     s->q = params->q;
     s->native = params->semantics == PLB_SEMANTICS_NATIVE;
     s->storage = params->storage;
+    s->aa = s->native && params->streaming == PLB_STREAMING_AA;
     s->graph_steps = graph_steps_default();
     int rc = PLB_OK;
     auto bail = [&](int code) { release(s); return code; };
@@ -496,7 +545,7 @@ int plb_solve_create(const plb_params* params, plb_solve** out) {
     // geometry
     Geo& g = s->g;
     g.nx = (int)params->nx; g.ny = (int)params->ny; g.nz = (int)params->nz;
-    const size_t esize = s->storage == PLB_STORAGE_FP16_DEV ? 2 : s->storage == PLB_STORAGE_FP64 ? 8 : 4;
+    const size_t esize = esize_of(s->storage);
     if (s->native) {
         g.h = 0; g.xoff = 0;
         g.ys = round_up(g.nx, 32 / (long long)esize);
@@ -521,9 +570,9 @@ int plb_solve_create(const plb_params* params, plb_solve** out) {
         const cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) return bail(fail(PLB_ECUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e)));
     }
-    const size_t pop_bytes = (size_t)s->q * (size_t)g.ks * esize;
-    if ((rc = dalloc(s, &s->f[0], pop_bytes)) != PLB_OK) return bail(rc);
-    if ((rc = dalloc(s, &s->f[1], pop_bytes)) != PLB_OK) return bail(rc);
+    const size_t pbytes = pop_bytes(s);
+    if ((rc = dalloc(s, &s->f[0], pbytes)) != PLB_OK) return bail(rc);
+    if (!s->aa && (rc = dalloc(s, &s->f[1], pbytes)) != PLB_OK) return bail(rc);   // AA: one buffer
     if ((rc = dalloc(s, (void**)&s->rho, (size_t)g.ks * sizeof(float))) != PLB_OK) return bail(rc);
     if ((rc = dalloc(s, (void**)&s->u, 3 * (size_t)g.ks * sizeof(float))) != PLB_OK) return bail(rc);
     if ((rc = dalloc(s, (void**)&s->consts, 2 * 27 * sizeof(float))) != PLB_OK) return bail(rc);
@@ -535,8 +584,8 @@ int plb_solve_create(const plb_params* params, plb_solve** out) {
     {
         // plbpd's SimData starts every field at 0 (src/SimData.cpp:53-56)
         cudaError_t e = cudaSuccess;
-        if (e == cudaSuccess) e = cudaMemsetAsync(s->f[0], 0, pop_bytes, s->stream);
-        if (e == cudaSuccess) e = cudaMemsetAsync(s->f[1], 0, pop_bytes, s->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s->f[0], 0, pbytes, s->stream);
+        if (e == cudaSuccess && s->f[1]) e = cudaMemsetAsync(s->f[1], 0, pbytes, s->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(s->rho, 0, (size_t)g.ks * sizeof(float), s->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(s->u, 0, 3 * (size_t)g.ks * sizeof(float), s->stream);
         if (e != cudaSuccess) return bail(fail(PLB_ECUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e)));
@@ -590,6 +639,22 @@ int plb_set_relaxation(plb_solve* s, float nu, const float* force3) {
     return PLB_OK;
 }
 
+int plb_set_collision(plb_solve* s, int32_t collision, float trt_magic) {
+    if (!s) return fail(PLB_EINVAL, "solve is null");
+    if (s->p.collision == collision && s->p.trt_magic == trt_magic) return PLB_OK;
+    plb_params p = s->p;
+    p.collision = collision;
+    p.trt_magic = trt_magic;
+    PLB_TRY(validate(&p));
+    PLB_TRY(set_device(s));
+    PLB_TRY(sync(s));
+    s->p.collision = collision;
+    s->p.trt_magic = trt_magic;
+    set_collision_params(s, s->p.nu, s->p.force);
+    drop_graphs(s);   // captured launches carry the old operator
+    return PLB_OK;
+}
+
 int plb_set_boundary(plb_solve* s, float rho_solid, const int32_t* face_type6, const int32_t* face_has_vel6,
                      const float* face_vel18) {
     if (!s || !face_type6 || !face_has_vel6 || !face_vel18) return fail(PLB_EINVAL, "null argument");
@@ -630,7 +695,7 @@ int plb_initialize(plb_solve* s) {
     if (!s) return fail(PLB_EINVAL, "solve is null");
     PLB_TRY(set_device(s));
     // Domain::initialize writes n, rho and u and leaves ntmp as it is
-    if (s->native) s->post = false;
+    if (s->native) { s->post = false; s->swapped = false; }
     PLB_KERNEL(util_init_uniform(s->q, s->storage, s->g, s->consts, s->p.rho0, s->p.u0, s->f[s->cur], nullptr,
                                  s->rho, s->u, s->stream));
     if (s->native) {
@@ -673,7 +738,7 @@ void* plb_stream_handle(plb_solve* s) { return s ? (void*)s->stream : nullptr; }
 
 int plb_collide(plb_solve* s) {
     PLB_REF_ONLY(s);
-    PLB_KERNEL(ref_collide(s->q, s->p.arith, s->g, s->cp, (float*)s->f[s->cur], s->rho, s->u, s->stream));
+    PLB_KERNEL(ref_collide(s->q, s->karith, s->g, s->cp, (float*)s->f[s->cur], s->rho, s->u, s->stream));
     return sync(s);
 }
 
@@ -738,9 +803,23 @@ int plb_get_field(plb_solve* s, int32_t which, float* out) {
     PLB_TRY(set_device(s));
     const size_t len = plb_field_len(s, which);
     int n_buf = s->cur;   // buffer that holds n for FIELD_N
+    void* tmp = nullptr;   // AA: transient natural copy of a swapped buffer
     if (s->native) {
         if (which == PLB_FIELD_NTMP) { std::memset(out, 0, len * sizeof(float)); return PLB_OK; }
-        if (s->post) {
+        if (s->post && s->aa) {
+            if (which == PLB_FIELD_N && s->swapped) {
+                PLB_CUDA(cudaMallocAsync(&tmp, pop_bytes(s), s->stream));
+                const int e = nat_aa_gather(s->q, s->storage, s->has_mask, true, s->g, s->np, s->f[0], tmp, nullptr,
+                                            nullptr, s->types, s->stream);
+                if (e != 0) {
+                    cudaFreeAsync(tmp, s->stream);
+                    return fail(PLB_ECUDA, std::string("nat_aa_gather: ") + cudaGetErrorString((cudaError_t)e));
+                }
+            } else if (which != PLB_FIELD_N) {
+                PLB_KERNEL(nat_aa_gather(s->q, s->storage, s->has_mask, s->swapped, s->g, s->np, s->f[0], nullptr,
+                                         s->rho, s->u, s->types, s->stream));
+            }
+        } else if (s->post) {
             PLB_TRY(nat_gather_to_other(s));
             n_buf = 1 - s->cur;
         }
@@ -750,8 +829,10 @@ int plb_get_field(plb_solve* s, int32_t which, float* out) {
     PLB_TRY(ensure_staging(s, (int)(len / ((size_t)(s->p.nx + 2) * (s->p.ny + 2) * (s->p.nz + 2)))));
     const float* wk = s->consts + s->q;
     if (which == PLB_FIELD_N || which == PLB_FIELD_NTMP) {
-        const void* src = s->f[which == PLB_FIELD_N ? n_buf : 1 - s->cur];
-        PLB_KERNEL(util_export(s->storage, s->q, s->g, src, wk, s->staging, s->stream));
+        const void* src = tmp ? tmp : s->f[which == PLB_FIELD_N ? n_buf : 1 - s->cur];
+        const int e = util_export(s->storage, s->q, s->g, src, wk, s->staging, s->stream);
+        if (tmp) cudaFreeAsync(tmp, s->stream);
+        if (e != 0) return fail(PLB_ECUDA, std::string("util_export: ") + cudaGetErrorString((cudaError_t)e));
     } else {
         PLB_KERNEL(util_export(0, which == PLB_FIELD_RHO ? 1 : 3, s->g, which == PLB_FIELD_RHO ? s->rho : s->u,
                                nullptr, s->staging, s->stream));
@@ -790,14 +871,28 @@ int plb_conservation(plb_solve* s, double* out4) {
     // the sums are of the current populations n_t; under NATIVE semantics the
     // state may be P_{t-1}, whose bounce-back slots hold reversed directions,
     // so n_t is gathered first (mass alone would not need it, momentum does)
-    int buf = s->cur;
-    if (s->native && s->post) {
+    const void* src = s->f[s->cur];
+    void* tmp = nullptr;
+    if (s->native && s->post && s->aa) {
+        if (s->swapped) {
+            PLB_CUDA(cudaMallocAsync(&tmp, pop_bytes(s), s->stream));
+            const int e = nat_aa_gather(s->q, s->storage, s->has_mask, true, s->g, s->np, s->f[0], tmp, nullptr,
+                                        nullptr, s->types, s->stream);
+            if (e != 0) {
+                cudaFreeAsync(tmp, s->stream);
+                return fail(PLB_ECUDA, std::string("nat_aa_gather: ") + cudaGetErrorString((cudaError_t)e));
+            }
+            src = tmp;
+        }
+    } else if (s->native && s->post) {
         PLB_KERNEL(nat_gather(s->q, s->storage, s->has_mask, s->g, s->np, s->f[s->cur], s->f[1 - s->cur], nullptr,
                               nullptr, s->types, s->stream));
-        buf = 1 - s->cur;
+        src = s->f[1 - s->cur];
     }
-    PLB_KERNEL(util_conservation(s->q, s->storage, s->g, s->f[buf], s->native ? s->types : nullptr,
-                                 s->fp.noslip_mask, s->partials, s->out4, s->stream));
+    const int ec = util_conservation(s->q, s->storage, s->g, src, s->native ? s->types : nullptr, s->fp.noslip_mask,
+                                     s->partials, s->out4, s->stream);
+    if (tmp) cudaFreeAsync(tmp, s->stream);
+    if (ec != 0) return fail(PLB_ECUDA, std::string("util_conservation: ") + cudaGetErrorString((cudaError_t)ec));
     PLB_CUDA(cudaMemcpyAsync(s->out4_host, s->out4, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
     PLB_TRY(sync(s));
     std::memcpy(out4, s->out4_host, 4 * sizeof(double));
@@ -926,6 +1021,7 @@ int plb_batch_create(int32_t n, plb_solve* const* solves, plb_batch** out) {
         if (s->q != s0->q || s->storage != s0->storage || s->karith != s0->karith || s->p.device != s0->p.device)
             return fail(PLB_EINVAL, "batch members must share lattice, storage, arithmetic and device");
         if (s->storage == PLB_STORAGE_FP64) return fail(PLB_EUNSUPPORTED, "FP64 storage is not batched");
+        if (s->aa) return fail(PLB_EUNSUPPORTED, "AA streaming is not batched");
         if ((long long)s->g.ys * s->g.ny * s->g.nz >= (1ll << 31))
             return fail(PLB_EINVAL, "batch member too large for 32-bit tile indices");
     }

@@ -75,6 +75,16 @@ int nat_fused_step(int q, int storage, int arith, bool has_mask, const Geo& g,
 int nat_gather(int q, int storage, bool has_mask, const Geo& g, const NativeParams& np,
                const void* src, void* n_out, float* rho, float* u, const uint8_t* types,
                cudaStream_t st);
+// AA in-place streaming on one buffer A: kind 0 = even step from a RAW state
+// (collides with the rho/u fields), 1 = even step, 2 = odd step.
+int nat_aa_step(int kind, int q, int storage, int arith, bool has_mask, const Geo& g, const CollideParams& cp,
+                const NativeParams& np, void* A, const float* rho, const float* u, const uint8_t* types,
+                cudaStream_t st);
+// Natural n (storage format, into n_out, or nullptr) and the moments with the
+// solid-node resets (rho/u, or nullptr) of an AA buffer; `swapped`: A holds
+// the layout an even step leaves.
+int nat_aa_gather(int q, int storage, bool has_mask, bool swapped, const Geo& g, const NativeParams& np,
+                  const void* A, void* n_out, float* rho, float* u, const uint8_t* types, cudaStream_t st);
 // Solid nodes' fields = (rho_solid, wall velocity).
 int nat_reset_fields(const Geo& g, const NativeParams& np, const uint8_t* types, float* rho,
                      float* u, cudaStream_t st);
@@ -109,6 +119,9 @@ int nat_fused_step_trt(int q, int storage, bool has_mask, const Geo& g, const Co
 int nat_collide_raw_trt(int q, int storage, bool has_mask, const Geo& g, const CollideParams& cp,
                         const NativeParams& np, const void* src, void* dst, const float* rho, const float* u,
                         const uint8_t* types, cudaStream_t st);
+int nat_aa_step_trt(int kind, int q, int storage, bool has_mask, const Geo& g, const CollideParams& cp,
+                    const NativeParams& np, void* A, const float* rho, const float* u, const uint8_t* types,
+                    cudaStream_t st);
 int nat_batch_blocks_per_sm_trt(int q, int storage, bool moving);
 int nat_batch_step_trt(int q, int storage, bool moving, const BatchDomain* doms, const int4* tiles, int ntiles,
                        int parity, int blocks, cudaStream_t st);

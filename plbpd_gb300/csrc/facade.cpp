@@ -17,6 +17,7 @@
 #include "../../include/plbpd/CalcMoments.hpp"
 #include "../../include/plbpd/Collision.hpp"
 #include "../../include/plbpd/CollisionSRT.hpp"
+#include "../../include/plbpd/CollisionTRT.hpp"
 #include "../../include/plbpd/Domain.hpp"
 #include "../../include/plbpd/EqlbDist.hpp"
 #include "../../include/plbpd/Flow.hpp"
@@ -58,8 +59,11 @@ plb_params base_params(const SimData& sd) {
     return p;
 }
 
-void install_collision(plb_solve* s, const Domain* d) {
+// The collision operator and its parameters: BGK for CollisionSRT (and the
+// fused march), TRT with its magic parameter for CollisionTRT.
+void install_collision(plb_solve* s, const Domain* d, int32_t collision = PLB_COLLISION_BGK, float magic = 0.0f) {
     const auto& F = d->get_external_force();
+    check(plb_set_collision(s, collision, magic), "plb_set_collision");
     check(plb_set_relaxation(s, d->get_fluid_viscosity(), F.data()), "plb_set_relaxation");
 }
 
@@ -363,6 +367,23 @@ void CollisionSRT::operator()(SimData& simdata, bool /*reference*/) const {
     const auto t0 = chrono::system_clock::now();
     plb_solve* s = simdata.device_for(base_params(simdata));
     install_collision(s, _domain);
+    check(plb_collide(s), "plb_collide");
+    simdata.mark_device_newer();
+    Collision::_time += seconds_since(t0);
+}
+
+// CollisionTRT: a second subclass of Collision (no counterpart in plbpd).
+CollisionTRT::CollisionTRT(const LBModel* lbmodel, const Domain* domain, float magic)
+    : _lbmodel(lbmodel), _domain(domain), _magic(magic) {
+    if (!(magic >= 0.0f)) throw std::invalid_argument("CollisionTRT: the magic parameter must be >= 0");
+}
+CollisionTRT::~CollisionTRT() {}
+float CollisionTRT::get_magic() const { return _magic > 0.0f ? _magic : 3.0f / 16.0f; }
+
+void CollisionTRT::operator()(SimData& simdata, bool /*reference*/) const {
+    const auto t0 = chrono::system_clock::now();
+    plb_solve* s = simdata.device_for(base_params(simdata));
+    install_collision(s, _domain, PLB_COLLISION_TRT, _magic);
     check(plb_collide(s), "plb_collide");
     simdata.mark_device_newer();
     Collision::_time += seconds_since(t0);

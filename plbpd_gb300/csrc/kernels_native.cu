@@ -113,6 +113,9 @@ int gather_q(int storage, bool m, const Geo& g, const NativeParams& np, const vo
     if (storage == 2)
         return m ? launch_gather<Q, 2, true>(g, np, src, n_out, rho, u, types, st)
                  : launch_gather<Q, 2, false>(g, np, src, n_out, rho, u, types, st);
+    if (storage == 3)
+        return m ? launch_gather<Q, 3, true>(g, np, src, n_out, rho, u, types, st)
+                 : launch_gather<Q, 3, false>(g, np, src, n_out, rho, u, types, st);
     return m ? launch_gather<Q, 0, true>(g, np, src, n_out, rho, u, types, st)
              : launch_gather<Q, 0, false>(g, np, src, n_out, rho, u, types, st);
 }
@@ -121,6 +124,49 @@ int gather_q(int storage, bool m, const Geo& g, const NativeParams& np, const vo
 int nat_gather(int q, int storage, bool has_mask, const Geo& g, const NativeParams& np, const void* src,
                void* n_out, float* rho, float* u, const uint8_t* types, cudaStream_t st) {
 #define CALL(Q) gather_q<Q>(storage, has_mask, g, np, src, n_out, rho, u, types, st)
+    return PLB_Q_DISPATCH(q, CALL);
+#undef CALL
+}
+
+int nat_aa_step(int kind, int q, int storage, int arith, bool has_mask, const Geo& g, const CollideParams& cp,
+                const NativeParams& np, void* A, const float* rho, const float* u, const uint8_t* types,
+                cudaStream_t st) {
+    if (arith == kArithTRT) return nat_aa_step_trt(kind, q, storage, has_mask, g, cp, np, A, rho, u, types, st);
+#define CALL(Q) aa_q<false, Q>(kind, storage, arith, has_mask, g, cp, np, A, rho, u, types, st)
+    return PLB_Q_DISPATCH(q, CALL);
+#undef CALL
+}
+
+namespace {
+template <int Q, int ST>
+int aa_gather_st(bool m, bool swapped, const Geo& g, const NativeParams& np, const void* A, void* n_out, float* rho,
+                 float* u, const uint8_t* types, cudaStream_t st) {
+    using T = typename Store<ST>::T;
+    const dim3 grid = row_grid<Q>(g, 32), block(32, kRows);
+    auto go = [&](auto mc, auto sc) {
+        nat_aa_gather_k<Q, ST, decltype(mc)::value, decltype(sc)::value><<<grid, block, 0, st>>>(
+            g, np, (const T*)A, (T*)n_out, rho, u, types);
+        return (int)cudaGetLastError();
+    };
+    if (m) return swapped ? go(std::true_type{}, std::true_type{}) : go(std::true_type{}, std::false_type{});
+    return swapped ? go(std::false_type{}, std::true_type{}) : go(std::false_type{}, std::false_type{});
+}
+
+template <int Q>
+int aa_gather_q(int storage, bool m, bool swapped, const Geo& g, const NativeParams& np, const void* A, void* n_out,
+                float* rho, float* u, const uint8_t* types, cudaStream_t st) {
+    switch (storage) {
+        case 1: return aa_gather_st<Q, 1>(m, swapped, g, np, A, n_out, rho, u, types, st);
+        case 2: return aa_gather_st<Q, 2>(m, swapped, g, np, A, n_out, rho, u, types, st);
+        case 3: return aa_gather_st<Q, 3>(m, swapped, g, np, A, n_out, rho, u, types, st);
+        default: return aa_gather_st<Q, 0>(m, swapped, g, np, A, n_out, rho, u, types, st);
+    }
+}
+}  // namespace
+
+int nat_aa_gather(int q, int storage, bool has_mask, bool swapped, const Geo& g, const NativeParams& np,
+                  const void* A, void* n_out, float* rho, float* u, const uint8_t* types, cudaStream_t st) {
+#define CALL(Q) aa_gather_q<Q>(storage, has_mask, swapped, g, np, A, n_out, rho, u, types, st)
     return PLB_Q_DISPATCH(q, CALL);
 #undef CALL
 }

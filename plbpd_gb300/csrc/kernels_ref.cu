@@ -274,6 +274,9 @@ int fused_dispatch(int arith, bool first, bool wb_all, const Geo& g, const Colli
     if (arith == kArithReference) {
         if (first) ref_fused_step_k<Q, kArithReference, true><<<grid, kBlockX, 0, st>>>(g, cp, fp, cur, nxt, rho, u, wb);
         else ref_fused_step_k<Q, kArithReference, false><<<grid, kBlockX, 0, st>>>(g, cp, fp, cur, nxt, rho, u, wb);
+    } else if (arith == kArithTRT) {
+        if (first) ref_fused_step_k<Q, kArithTRT, true><<<grid, kBlockX, 0, st>>>(g, cp, fp, cur, nxt, rho, u, wb);
+        else ref_fused_step_k<Q, kArithTRT, false><<<grid, kBlockX, 0, st>>>(g, cp, fp, cur, nxt, rho, u, wb);
     } else {
         if (first) ref_fused_step_k<Q, kArithFP32, true><<<grid, kBlockX, 0, st>>>(g, cp, fp, cur, nxt, rho, u, wb);
         else ref_fused_step_k<Q, kArithFP32, false><<<grid, kBlockX, 0, st>>>(g, cp, fp, cur, nxt, rho, u, wb);
@@ -329,6 +332,7 @@ int ref_collide(int q, int arith, const Geo& g, const CollideParams& cp, float* 
     const dim3 grid = cell_grid(g);
 #define CALL(Q) (arith == kArithReference \
     ? (ref_collide_k<Q, kArithReference><<<grid, kBlockX, 0, st>>>(g, cp, n, rho, u), 0) \
+    : arith == kArithTRT ? (ref_collide_k<Q, kArithTRT><<<grid, kBlockX, 0, st>>>(g, cp, n, rho, u), 0) \
     : (ref_collide_k<Q, kArithFP32><<<grid, kBlockX, 0, st>>>(g, cp, n, rho, u), 0), (int)cudaGetLastError())
     return PLB_Q_DISPATCH(q, CALL);
 #undef CALL

@@ -19,6 +19,14 @@ int nat_collide_raw_trt(int q, int storage, bool has_mask, const Geo& g, const C
 #undef CALL
 }
 
+int nat_aa_step_trt(int kind, int q, int storage, bool has_mask, const Geo& g, const CollideParams& cp,
+                    const NativeParams& np, void* A, const float* rho, const float* u, const uint8_t* types,
+                    cudaStream_t st) {
+#define CALL(Q) aa_q<true, Q>(kind, storage, kArithTRT, has_mask, g, cp, np, A, rho, u, types, st)
+    return PLB_Q_DISPATCH(q, CALL);
+#undef CALL
+}
+
 int nat_batch_blocks_per_sm_trt(int q, int storage, bool moving) {
     return batch_blocks_per_sm<true>(q, storage, kArithTRT, moving);
 }

@@ -9,7 +9,8 @@ constexpr int kBlock = 256;
 
 // Domain::initialize (src/Domain.cpp:46-63): every node of the box, halo
 // included, gets rho0, u0 and the equilibrium; ntmp starts at zero
-// (src/SimData.cpp:53-56).  Under FP16 storage the buffers hold f - w.
+// (src/SimData.cpp:53-56).  Under FP16 and FP32 deviation storage the
+// buffers hold f - w.
 template <int ST>
 __global__ void init_uniform_k(Geo g, int q, const float* __restrict__ feq, const float* __restrict__ wk,
                                float rho0, float u0x, float u0y, float u0z, void* __restrict__ n,
@@ -25,6 +26,9 @@ __global__ void init_uniform_k(Geo g, int q, const float* __restrict__ feq, cons
         } else if (ST == 1) {
             static_cast<__half*>(n)[k * g.ks + i] = __float2half_rn(__fsub_rn(feq[k], wk[k]));
             if (nt) static_cast<__half*>(nt)[k * g.ks + i] = __float2half_rn(-wk[k]);
+        } else if (ST == 3) {
+            static_cast<float*>(n)[k * g.ks + i] = __fsub_rn(feq[k], wk[k]);
+            if (nt) static_cast<float*>(nt)[k * g.ks + i] = -wk[k];
         } else {
             static_cast<double*>(n)[k * g.ks + i] = (double)feq[k];
             if (nt) static_cast<double*>(nt)[k * g.ks + i] = 0.0;
@@ -51,6 +55,7 @@ __global__ void export_k(Geo g, int v, const void* __restrict__ src, const float
         if (held) {
             if (ST == 0) val = static_cast<const float*>(src)[c * g.ks + node];
             else if (ST == 1) val = __fadd_rn(__half2float(static_cast<const __half*>(src)[c * g.ks + node]), wk[c]);
+            else if (ST == 3) val = __fadd_rn(static_cast<const float*>(src)[c * g.ks + node], wk[c]);
             else val = __double2float_rn(static_cast<const double*>(src)[c * g.ks + node]);
         }
         aos[i * v + c] = val;
@@ -72,6 +77,7 @@ __global__ void import_k(Geo g, int v, const float* __restrict__ aos, const floa
         const float val = aos[i * v + c];
         if (ST == 0) static_cast<float*>(dst)[c * g.ks + node] = val;
         else if (ST == 1) static_cast<__half*>(dst)[c * g.ks + node] = __float2half_rn(__fsub_rn(val, wk[c]));
+        else if (ST == 3) static_cast<float*>(dst)[c * g.ks + node] = __fsub_rn(val, wk[c]);
         else static_cast<double*>(dst)[c * g.ks + node] = (double)val;
     }
 }
@@ -106,6 +112,7 @@ conservation_k(Geo g, const void* __restrict__ n, const uint8_t* __restrict__ ty
             double v;
             if (ST == 0) v = (double)static_cast<const float*>(n)[k * g.ks + node];
             else if (ST == 1) v = (double)__half2float(static_cast<const __half*>(n)[k * g.ks + node]) + (double)weight<Q>(k);
+            else if (ST == 3) v = (double)static_cast<const float*>(n)[k * g.ks + node] + (double)weight<Q>(k);
             else v = static_cast<const double*>(n)[k * g.ks + node];
             m += v;
             if (Lattice<Q>::cx(k)) px += Lattice<Q>::cx(k) * v;
@@ -160,6 +167,8 @@ int util_init_uniform(int q, int storage, const Geo& g, const float* feq_dev, fl
         init_uniform_k<0><<<blocks_for(g.fs), kBlock, 0, st>>>(g, q, feq_dev, wk, rho0, u0[0], u0[1], u0[2], n, nt, rho, u);
     else if (storage == 1)
         init_uniform_k<1><<<blocks_for(g.fs), kBlock, 0, st>>>(g, q, feq_dev, wk, rho0, u0[0], u0[1], u0[2], n, nt, rho, u);
+    else if (storage == 3)
+        init_uniform_k<3><<<blocks_for(g.fs), kBlock, 0, st>>>(g, q, feq_dev, wk, rho0, u0[0], u0[1], u0[2], n, nt, rho, u);
     else
         init_uniform_k<2><<<blocks_for(g.fs), kBlock, 0, st>>>(g, q, feq_dev, wk, rho0, u0[0], u0[1], u0[2], n, nt, rho, u);
     return (int)cudaGetLastError();
@@ -169,6 +178,7 @@ int util_export(int storage, int v, const Geo& g, const void* src, const float* 
     const long long cells = (long long)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
     if (storage == 0) export_k<0><<<blocks_for(cells), kBlock, 0, st>>>(g, v, src, wk, aos);
     else if (storage == 1) export_k<1><<<blocks_for(cells), kBlock, 0, st>>>(g, v, src, wk, aos);
+    else if (storage == 3) export_k<3><<<blocks_for(cells), kBlock, 0, st>>>(g, v, src, wk, aos);
     else export_k<2><<<blocks_for(cells), kBlock, 0, st>>>(g, v, src, wk, aos);
     return (int)cudaGetLastError();
 }
@@ -177,6 +187,7 @@ int util_import(int storage, int v, const Geo& g, const float* aos, const float*
     const long long cells = (long long)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
     if (storage == 0) import_k<0><<<blocks_for(cells), kBlock, 0, st>>>(g, v, aos, wk, dst);
     else if (storage == 1) import_k<1><<<blocks_for(cells), kBlock, 0, st>>>(g, v, aos, wk, dst);
+    else if (storage == 3) import_k<3><<<blocks_for(cells), kBlock, 0, st>>>(g, v, aos, wk, dst);
     else import_k<2><<<blocks_for(cells), kBlock, 0, st>>>(g, v, aos, wk, dst);
     return (int)cudaGetLastError();
 }
@@ -191,6 +202,7 @@ int util_conservation(int q, int storage, const Geo& g, const void* n, const uin
     if (nb < 1) nb = 1;
 #define CALL(Q) (storage == 0 ? (conservation_k<Q, 0><<<nb, kBlock, 0, st>>>(g, n, types, noslip_mask, partials), 0) \
              : storage == 1 ? (conservation_k<Q, 1><<<nb, kBlock, 0, st>>>(g, n, types, noslip_mask, partials), 0) \
+             : storage == 3 ? (conservation_k<Q, 3><<<nb, kBlock, 0, st>>>(g, n, types, noslip_mask, partials), 0) \
                             : (conservation_k<Q, 2><<<nb, kBlock, 0, st>>>(g, n, types, noslip_mask, partials), 0))
     if (q == 9) CALL(9);
     else if (q == 19) CALL(19);

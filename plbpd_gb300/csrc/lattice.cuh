@@ -199,10 +199,68 @@ __device__ __forceinline__ float dot_c(int k, float ux, float uy, float uz) {
 //   tail (k >= 8*floor(Q/8), REFERENCE arithmetic only): the bracket
 //         1 + 3cu + 4.5cu^2 - 1.5usq in FP64 times the float w*rho, then
 //         (1-omega)*n (float) + omega*neq in FP64, rounded to float.
-// Under kArithFP32 the body's sequence is used for every direction.
+// ---- TRT ----------------------------------------------------------------------
+// Two relaxation times with a second-order force source (the oracle's
+// orc_set_trt states the method); pairs (k, k + 1) with k odd are opposite
+// directions.  DEV: populations are deviations d = f - w (FP16 storage), so
+// the even equilibrium enters as e+ - w = w (drho + rho (4.5cu^2 - 1.5usq)).
+// Op order, FP32:
+//   hr = 0.5/rho; v = u + F hr; vsq = (vx^2 + vy^2) + vz^2; uF = (vx Fx + vy Fy) + vz Fz
+//   kusq = -1.5 vsq; base = 1 + kusq; m3uF = -3 uF
+//   e0 = (w0 rho) base | fma(w0 rho, kusq, w0 drho);  n0 = (n0 - om (n0 - e0)) + (gp w0) m3uF
+//   per pair: t = 4.5 cu; e+ = (w rho) fma(t, cu, base) | fma(w rho, fma(t, cu, kusq), w drho)
+//     e- = (w rho)(3 cu); s+ = 0.5 (nk + nr); s- = 0.5 (nk - nr)
+//     a = om (s+ - e+); b = omm (s- - e-); S+ = (gp w) fma(9 cu, cF, m3uF); S- = (gm w)(3 cF)
+//     nk = ((nk - a) - b) + (S+ + S-); nr = ((nr - a) + b) + (S+ - S-)
+template <int Q, bool DEV>
+__device__ __forceinline__ void collide_node_trt(float (&f)[Q], float drho, float rho, float ux, float uy, float uz,
+                                                 const CollideParams& P) {
+    const float hr = __fdiv_rn(0.5f, rho);
+    const float vx = __fadd_rn(ux, __fmul_rn(P.fx, hr));
+    const float vy = __fadd_rn(uy, __fmul_rn(P.fy, hr));
+    const float vz = __fadd_rn(uz, __fmul_rn(P.fz, hr));
+    const float vsq = __fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz));
+    const float uF = __fadd_rn(__fadd_rn(__fmul_rn(vx, P.fx), __fmul_rn(vy, P.fy)), __fmul_rn(vz, P.fz));
+    const float kusq = __fmul_rn(-1.5f, vsq);
+    const float base = __fadd_rn(1.0f, kusq);
+    const float m3uF = __fmul_rn(-3.0f, uF);
+    const float om = P.omega, omm = P.omega_m;
+    {
+        const float w0 = weight<Q>(0), wr0 = __fmul_rn(w0, rho);
+        const float e0 = DEV ? __fmaf_rn(wr0, kusq, __fmul_rn(w0, drho)) : __fmul_rn(wr0, base);
+        f[0] = __fadd_rn(__fsub_rn(f[0], __fmul_rn(om, __fsub_rn(f[0], e0))), __fmul_rn(__fmul_rn(P.gp, w0), m3uF));
+    }
+#pragma unroll
+    for (int k = 1; k < Q; k += 2) {
+        const float w = weight<Q>(k), wr = __fmul_rn(w, rho);
+        const float cu = dot_c<Q>(k, vx, vy, vz);
+        const float cF = dot_c<Q>(k, P.fx, P.fy, P.fz);
+        const float t = __fmul_rn(4.5f, cu);
+        const float ep = DEV ? __fmaf_rn(wr, __fmaf_rn(t, cu, kusq), __fmul_rn(w, drho))
+                             : __fmul_rn(wr, __fmaf_rn(t, cu, base));
+        const float em = __fmul_rn(wr, __fmul_rn(3.0f, cu));
+        const float sp = __fmul_rn(0.5f, __fadd_rn(f[k], f[k + 1]));
+        const float sm = __fmul_rn(0.5f, __fsub_rn(f[k], f[k + 1]));
+        const float a = __fmul_rn(om, __fsub_rn(sp, ep));
+        const float b = __fmul_rn(omm, __fsub_rn(sm, em));
+        const float Sp = __fmul_rn(__fmul_rn(P.gp, w), __fmaf_rn(__fmul_rn(9.0f, cu), cF, m3uF));
+        const float Sm = __fmul_rn(__fmul_rn(P.gm, w), __fmul_rn(3.0f, cF));
+        const float nk = __fadd_rn(__fsub_rn(__fsub_rn(f[k], a), b), __fadd_rn(Sp, Sm));
+        const float nr = __fadd_rn(__fadd_rn(__fsub_rn(f[k + 1], a), b), __fsub_rn(Sp, Sm));
+        f[k] = nk;
+        f[k + 1] = nr;
+    }
+}
+
+// Under kArithFP32 the body's sequence is used for every direction; under
+// kArithTRT the two-relaxation-time operator above replaces BGK.
 template <int Q, int ARITH>
 __device__ __forceinline__ void collide_node(float (&f)[Q], float rho, float ux, float uy, float uz,
                                              const CollideParams& P) {
+    if constexpr (ARITH == kArithTRT) {
+        collide_node_trt<Q, false>(f, 0.0f, rho, ux, uy, uz, P);
+        return;
+    }
     const float tr = __fdiv_rn(P.tau, rho);
     const float vx = __fadd_rn(ux, __fmul_rn(P.fx, tr));
     const float vy = __fadd_rn(uy, __fmul_rn(P.fy, tr));

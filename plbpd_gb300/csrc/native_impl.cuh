@@ -19,6 +19,8 @@
 //   1  FP16 deviations d_k = f_k - w_k, arithmetic in FP32 in deviation form
 //   2  FP64 populations and FP64 arithmetic: the reference run of the same
 //      method that reduced-precision runs are measured against
+//   3  FP32 deviations d_k = f_k - w_k, FP16's arithmetic without its rounding:
+//      FP32 cost, with the precision kept where the flow is (f - w is small)
 #pragma once
 
 #include <type_traits>
@@ -30,40 +32,74 @@ namespace {
 
 constexpr int kBlockX = 128;
 
+// Thread blocks of the per-node kernels are 32 x kRows: each warp takes 32
+// consecutive x (64 for the FP16 pair kernel) of one row, so a row of any
+// length leaves at most one warp partly idle.  Rows run along y for the 3-D
+// lattices and along z for D2Q9, whose domains are one node thick in y.
+constexpr int kRows = kBlockX / 32;
+
+template <int Q>
+__device__ __forceinline__ void row_of(int& y, int& z) {
+    if (Q == 9) { y = blockIdx.y; z = blockIdx.z * kRows + threadIdx.y; }
+    else { y = blockIdx.y * kRows + threadIdx.y; z = blockIdx.z; }
+}
+
+template <int Q>
+dim3 row_grid(const Geo& g, int x_per_warp) {
+    const unsigned gx = (unsigned)((g.nx + x_per_warp - 1) / x_per_warp);
+    return Q == 9 ? dim3(gx, (unsigned)g.ny, (unsigned)((g.nz + kRows - 1) / kRows))
+                  : dim3(gx, (unsigned)((g.ny + kRows - 1) / kRows), (unsigned)g.nz);
+}
+
+// Storage accessors: ld reads through the read-only path (buffers the kernel
+// does not write), ldp is a plain load (the in-place AA kernels), st streams.
 template <int ST> struct Store;
 template <> struct Store<0> {
     using T = float;
     using R = float;
     __device__ static __forceinline__ float ld(const float* p, long long i) { return __ldg(p + i); }
+    __device__ static __forceinline__ float ldp(const float* p, long long i) { return p[i]; }
     __device__ static __forceinline__ void st(float* p, long long i, float v) { __stcs(p + i, v); }
 };
 template <> struct Store<1> {
     using T = __half;
     using R = float;
     __device__ static __forceinline__ float ld(const __half* p, long long i) { return __half2float(__ldg(p + i)); }
+    __device__ static __forceinline__ float ldp(const __half* p, long long i) { return __half2float(p[i]); }
     __device__ static __forceinline__ void st(__half* p, long long i, float v) {
         __stcs(reinterpret_cast<unsigned short*>(p) + i, __half_as_ushort(__float2half_rn(v)));
     }
+};
+// FP32 deviations d = f - w: the FP16 storage's arithmetic without its rounding
+template <> struct Store<3> {
+    using T = float;
+    using R = float;
+    __device__ static __forceinline__ float ld(const float* p, long long i) { return __ldg(p + i); }
+    __device__ static __forceinline__ float ldp(const float* p, long long i) { return p[i]; }
+    __device__ static __forceinline__ void st(float* p, long long i, float v) { __stcs(p + i, v); }
 };
 template <> struct Store<2> {
     using T = double;
     using R = double;
     __device__ static __forceinline__ double ld(const double* p, long long i) { return __ldg(p + i); }
+    __device__ static __forceinline__ double ldp(const double* p, long long i) { return p[i]; }
     __device__ static __forceinline__ void st(double* p, long long i, double v) { __stcs(p + i, v); }
 };
 
 // Neighbour index helper: element offsets of x-1, x, x+1 (and y, z) with the
 // periodic axes wrapped.  A fluid node never has a neighbour outside the box
-// along a walled axis, because the wall layer in between is solid.
+// along a walled axis, because the wall layer in between is solid; for the
+// wall layer itself such a neighbour is clamped to the node's own row, so
+// that kernels may load a node's sources before they know it is solid.
 struct Nbr {
     long long xo[3], yo[3], zo[3];
     __device__ __forceinline__ Nbr(const Geo& g, int x, int y, int z) {
-        const int xm = (x == 0 && g.wrap_x) ? g.nx - 1 : x - 1;
-        const int xp = (x == g.nx - 1 && g.wrap_x) ? 0 : x + 1;
-        const int ym = (y == 0 && g.wrap_y) ? g.ny - 1 : y - 1;
-        const int yp = (y == g.ny - 1 && g.wrap_y) ? 0 : y + 1;
-        const int zm = (z == 0 && g.wrap_z) ? g.nz - 1 : z - 1;
-        const int zp = (z == g.nz - 1 && g.wrap_z) ? 0 : z + 1;
+        const int xm = x == 0 ? (g.wrap_x ? g.nx - 1 : x) : x - 1;
+        const int xp = x == g.nx - 1 ? (g.wrap_x ? 0 : x) : x + 1;
+        const int ym = y == 0 ? (g.wrap_y ? g.ny - 1 : y) : y - 1;
+        const int yp = y == g.ny - 1 ? (g.wrap_y ? 0 : y) : y + 1;
+        const int zm = z == 0 ? (g.wrap_z ? g.nz - 1 : z) : z - 1;
+        const int zp = z == g.nz - 1 ? (g.wrap_z ? 0 : z) : z + 1;
         xo[0] = xm + g.xoff; xo[1] = x + g.xoff; xo[2] = xp + g.xoff;
         yo[0] = (long long)ym * g.ys; yo[1] = (long long)y * g.ys; yo[2] = (long long)yp * g.ys;
         zo[0] = (long long)zm * g.zs; zo[1] = (long long)z * g.zs; zo[2] = (long long)zp * g.zs;
@@ -180,59 +216,7 @@ __device__ __forceinline__ void collide_node_d(double (&f)[Q], double rho, doubl
     }
 }
 
-// ---- TRT ----------------------------------------------------------------------
-// Two relaxation times with a second-order force source (the oracle's
-// orc_set_trt states the method); pairs (k, k + 1) with k odd are opposite
-// directions.  DEV: populations are deviations d = f - w (FP16 storage), so
-// the even equilibrium enters as e+ - w = w (drho + rho (4.5cu^2 - 1.5usq)).
-// Op order, FP32:
-//   hr = 0.5/rho; v = u + F hr; vsq = (vx^2 + vy^2) + vz^2; uF = (vx Fx + vy Fy) + vz Fz
-//   kusq = -1.5 vsq; base = 1 + kusq; m3uF = -3 uF
-//   e0 = (w0 rho) base | fma(w0 rho, kusq, w0 drho);  n0 = (n0 - om (n0 - e0)) + (gp w0) m3uF
-//   per pair: t = 4.5 cu; e+ = (w rho) fma(t, cu, base) | fma(w rho, fma(t, cu, kusq), w drho)
-//     e- = (w rho)(3 cu); s+ = 0.5 (nk + nr); s- = 0.5 (nk - nr)
-//     a = om (s+ - e+); b = omm (s- - e-); S+ = (gp w) fma(9 cu, cF, m3uF); S- = (gm w)(3 cF)
-//     nk = ((nk - a) - b) + (S+ + S-); nr = ((nr - a) + b) + (S+ - S-)
-template <int Q, bool DEV>
-__device__ __forceinline__ void collide_node_trt(float (&f)[Q], float drho, float rho, float ux, float uy, float uz,
-                                                 const CollideParams& P) {
-    const float hr = __fdiv_rn(0.5f, rho);
-    const float vx = __fadd_rn(ux, __fmul_rn(P.fx, hr));
-    const float vy = __fadd_rn(uy, __fmul_rn(P.fy, hr));
-    const float vz = __fadd_rn(uz, __fmul_rn(P.fz, hr));
-    const float vsq = __fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz));
-    const float uF = __fadd_rn(__fadd_rn(__fmul_rn(vx, P.fx), __fmul_rn(vy, P.fy)), __fmul_rn(vz, P.fz));
-    const float kusq = __fmul_rn(-1.5f, vsq);
-    const float base = __fadd_rn(1.0f, kusq);
-    const float m3uF = __fmul_rn(-3.0f, uF);
-    const float om = P.omega, omm = P.omega_m;
-    {
-        const float w0 = weight<Q>(0), wr0 = __fmul_rn(w0, rho);
-        const float e0 = DEV ? __fmaf_rn(wr0, kusq, __fmul_rn(w0, drho)) : __fmul_rn(wr0, base);
-        f[0] = __fadd_rn(__fsub_rn(f[0], __fmul_rn(om, __fsub_rn(f[0], e0))), __fmul_rn(__fmul_rn(P.gp, w0), m3uF));
-    }
-#pragma unroll
-    for (int k = 1; k < Q; k += 2) {
-        const float w = weight<Q>(k), wr = __fmul_rn(w, rho);
-        const float cu = dot_c<Q>(k, vx, vy, vz);
-        const float cF = dot_c<Q>(k, P.fx, P.fy, P.fz);
-        const float t = __fmul_rn(4.5f, cu);
-        const float ep = DEV ? __fmaf_rn(wr, __fmaf_rn(t, cu, kusq), __fmul_rn(w, drho))
-                             : __fmul_rn(wr, __fmaf_rn(t, cu, base));
-        const float em = __fmul_rn(wr, __fmul_rn(3.0f, cu));
-        const float sp = __fmul_rn(0.5f, __fadd_rn(f[k], f[k + 1]));
-        const float sm = __fmul_rn(0.5f, __fsub_rn(f[k], f[k + 1]));
-        const float a = __fmul_rn(om, __fsub_rn(sp, ep));
-        const float b = __fmul_rn(omm, __fsub_rn(sm, em));
-        const float Sp = __fmul_rn(__fmul_rn(P.gp, w), __fmaf_rn(__fmul_rn(9.0f, cu), cF, m3uF));
-        const float Sm = __fmul_rn(__fmul_rn(P.gm, w), __fmul_rn(3.0f, cF));
-        const float nk = __fadd_rn(__fsub_rn(__fsub_rn(f[k], a), b), __fadd_rn(Sp, Sm));
-        const float nr = __fadd_rn(__fadd_rn(__fsub_rn(f[k + 1], a), b), __fsub_rn(Sp, Sm));
-        f[k] = nk;
-        f[k + 1] = nr;
-    }
-}
-
+// ---- TRT, FP64 storage (the FP32 operator is collide_node_trt in lattice.cuh) ----
 // The same in double (FP64 storage): omega = 1/tau and gp = 1 - omega/2 in
 // double, omm = omega_m_d, gm = 1 - omm/2; e+ = (w rho)((1 + (4.5cu)cu) - 1.5vsq),
 // S+ = (gp w)((9cu) cF + m3uF); otherwise the FP32 order.
@@ -281,9 +265,8 @@ __device__ __forceinline__ void collide_any(typename Store<ST>::R (&f)[Q], typen
                                             typename Store<ST>::R ux, typename Store<ST>::R uy,
                                             typename Store<ST>::R uz, float drho, const CollideParams& cp) {
     if constexpr (ST == 0) {
-        if constexpr (ARITH == kArithTRT) collide_node_trt<Q, false>(f, 0.0f, rho, ux, uy, uz, cp);
-        else collide_node<Q, ARITH>(f, rho, ux, uy, uz, cp);
-    } else if constexpr (ST == 1) {
+        collide_node<Q, ARITH>(f, rho, ux, uy, uz, cp);
+    } else if constexpr (ST == 1 || ST == 3) {
         if constexpr (ARITH == kArithTRT) collide_node_trt<Q, true>(f, drho, rho, ux, uy, uz, cp);
         else collide_node_dev<Q>(f, drho, rho, ux, uy, uz, cp);
     } else {
@@ -299,7 +282,7 @@ __device__ __forceinline__ void update_node(typename Store<ST>::R (&f)[Q], typen
         float ux, uy, uz;
         node_moments<Q>(f, rho, ux, uy, uz);
         collide_any<Q, ST, ARITH>(f, rho, ux, uy, uz, 0.0f, cp);
-    } else if constexpr (ST == 1) {
+    } else if constexpr (ST == 1 || ST == 3) {
         float drho, ux, uy, uz;
         node_moments_dev<Q>(f, drho, rho, ux, uy, uz);
         collide_any<Q, ST, ARITH>(f, rho, ux, uy, uz, drho, cp);
@@ -315,7 +298,7 @@ __device__ __forceinline__ void moments_any(const typename Store<ST>::R (&f)[Q],
                                             typename Store<ST>::R& ux, typename Store<ST>::R& uy,
                                             typename Store<ST>::R& uz) {
     if constexpr (ST == 0) node_moments<Q>(f, rho, ux, uy, uz);
-    else if constexpr (ST == 1) { float drho; node_moments_dev<Q>(f, drho, rho, ux, uy, uz); }
+    else if constexpr (ST == 1 || ST == 3) { float drho; node_moments_dev<Q>(f, drho, rho, ux, uy, uz); }
     else node_moments_d<Q>(f, rho, ux, uy, uz);
 }
 
@@ -361,22 +344,35 @@ __device__ __forceinline__ uint32_t links_of(const uint8_t t, const uint32_t* __
     return (MASK && (t & kNearSolid)) ? __ldg(links + node) : 0u;
 }
 
-// Gathers n[x][*] from P (streaming plus bounce-back).  `links` bit k is set
-// when x + c_k is solid, so the source x - c_k is solid when bit rev(k) is.
-template <int Q, int ST, bool MASK>
-__device__ __forceinline__ void gather_node(const typename Store<ST>::T* __restrict__ src, const Geo& g,
-                                            uint32_t links, const Nbr& nb, long long node,
-                                            typename Store<ST>::R (&f)[Q]) {
-    // every source is inside the box (a solid source is a node too), so the
-    // streaming loads are unconditional; bounce-back directions are then
-    // replaced by the node's own reversed slot
+// Gathers n[x][*] from P: the streaming loads, then the bounce-back fix-up.
+// Every source address is inside the box (a solid source is a node too, and
+// Nbr clamps at walled faces), so the streaming loads are unconditional and
+// are issued before the node's type is known; bounce-back directions are then
+// replaced by the node's own reversed slot.  `links` bit k is set when
+// x + c_k is solid, so the source x - c_k is solid when bit rev(k) is.
+template <int Q, int ST>
+__device__ __forceinline__ void stream_loads(const typename Store<ST>::T* __restrict__ src, const Geo& g,
+                                             const Nbr& nb, typename Store<ST>::R (&f)[Q]) {
 #pragma unroll
     for (int k = 0; k < Q; ++k) f[k] = Store<ST>::ld(src, k * g.ks + nb.at<Q>(k, -1));
-    if (MASK && links) {
+}
+
+template <int Q, int ST>
+__device__ __forceinline__ void bounce_fixup(const typename Store<ST>::T* __restrict__ src, const Geo& g,
+                                             uint32_t links, long long node, typename Store<ST>::R (&f)[Q]) {
+    if (links) {
 #pragma unroll
         for (int k = 1; k < Q; ++k)
             if ((links >> rev_of(k)) & 1u) f[k] = Store<ST>::ld(src, rev_of(k) * g.ks + node);
     }
+}
+
+template <int Q, int ST, bool MASK>
+__device__ __forceinline__ void gather_node(const typename Store<ST>::T* __restrict__ src, const Geo& g,
+                                            uint32_t links, const Nbr& nb, long long node,
+                                            typename Store<ST>::R (&f)[Q]) {
+    stream_loads<Q, ST>(src, g, nb, f);
+    if (MASK) bounce_fixup<Q, ST>(src, g, links, node, f);
 }
 
 // ---------------------------------------------------------------------------
@@ -385,19 +381,23 @@ __global__ void __launch_bounds__(kBlockX)
 nat_fused_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::T* __restrict__ src,
             typename Store<ST>::T* __restrict__ dst, const uint8_t* __restrict__ types) {
     using R = typename Store<ST>::R;
-    const int x = blockIdx.x * kBlockX + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
-    if (x >= g.nx) return;
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    int y, z;
+    row_of<Q>(y, z);
+    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
     const long long node = g.idx(x, y, z);
+    const Nbr nb(g, x, y, z);
+    // the type and the streaming loads are issued together: waiting for the
+    // type first would add a memory round trip before the loads
+    const uint8_t t = MASK ? __ldg(types + node) : 0;
+    R f[Q];
+    stream_loads<Q, ST>(src, g, nb, f);
     uint32_t L = 0;
     if (MASK) {
-        const uint8_t t = __ldg(types + node);
         if (t & kSolid) return;
         L = links_of<MASK>(t, np.links, node);
+        bounce_fixup<Q, ST>(src, g, L, node, f);
     }
-    const Nbr nb(g, x, y, z);
-    R f[Q];
-    gather_node<Q, ST, MASK>(src, g, L, nb, node, f);
     R rho;
     update_node<Q, ST, ARITH>(f, rho, cp);
     store_node<Q, ST, MASK>(dst, g, np, types, L, nb, node, rho, f);
@@ -425,9 +425,11 @@ __global__ void __launch_bounds__(kBlockX)
 nat_fused_h2_k(Geo g, CollideParams cp, NativeParams np, const __half* __restrict__ src, __half* __restrict__ dst,
                const uint8_t* __restrict__ types) {
     const unsigned kFull = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const int x0 = 2 * (blockIdx.x * kBlockX + threadIdx.x);
-    const int y = blockIdx.y, z = blockIdx.z;
+    const int lane = threadIdx.x;   // blockDim.x is 32: a warp is one row
+    const int x0 = 2 * (blockIdx.x * 32 + threadIdx.x);
+    int y, z;
+    row_of<Q>(y, z);
+    if (y >= g.ny || z >= g.nz) return;   // the whole warp: no shuffle is left half done
     const bool active = x0 < g.nx;
     const int ym = y == 0 ? (g.wrap_y ? g.ny - 1 : y) : y - 1;
     const int yp = y == g.ny - 1 ? (g.wrap_y ? 0 : y) : y + 1;
@@ -518,9 +520,10 @@ nat_collide_raw_k(Geo g, CollideParams cp, NativeParams np, const typename Store
                   typename Store<ST>::T* __restrict__ dst, const float* __restrict__ rho_f,
                   const float* __restrict__ u_f, const uint8_t* __restrict__ types) {
     using R = typename Store<ST>::R;
-    const int x = blockIdx.x * kBlockX + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
-    if (x >= g.nx) return;
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    int y, z;
+    row_of<Q>(y, z);
+    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
     const long long node = g.idx(x, y, z);
     uint32_t L = 0;
     if (MASK) {
@@ -534,8 +537,156 @@ nat_collide_raw_k(Geo g, CollideParams cp, NativeParams np, const typename Store
     for (int k = 0; k < Q; ++k) f[k] = Store<ST>::ld(src, k * g.ks + node);
     const R rho = (R)rho_f[node];
     const R ux = (R)u_f[node], uy = (R)u_f[g.ks + node], uz = (R)u_f[2 * g.ks + node];
-    collide_any<Q, ST, ARITH>(f, rho, ux, uy, uz, ST == 1 ? __fsub_rn((float)rho, 1.0f) : 0.0f, cp);
+    collide_any<Q, ST, ARITH>(f, rho, ux, uy, uz, (ST == 1 || ST == 3) ? __fsub_rn((float)rho, 1.0f) : 0.0f, cp);
     store_node<Q, ST, MASK>(dst, g, np, types, L, nb, node, rho, f);
+}
+
+// ---- AA in-place streaming (one population buffer) ----------------------------
+// Even step at node x: reads its own slots A[k][x] = n_k(x), collides, stores
+// n*_k in A[rev k][x]; no neighbour is touched.  Odd step: gathers
+// n_k(x) = A[rev k][x - c_k] (the even step's n*_k(x - c_k)), or A[k][x] when
+// x - c_k is solid (x's own n*_{rev k}, bounced); collides; stores n*_k in
+// A[k][x + c_k], or in A[rev k][x] when x + c_k is solid, where x's next even
+// step reads it back as n_{rev k}.  Either step reads exactly the slots the
+// same thread writes, so the update is in place without races, and after an
+// odd step A holds the pre-collision populations in the natural layout.
+// Bounce-back values carry the moving-wall term when stored.  Every value is
+// the one the two-buffer kernel computes, so the two are bit-identical.
+template <int Q, int ST, bool MASK, int ARITH, bool MOVING, bool RAW>
+__global__ void __launch_bounds__(kBlockX)
+nat_aa_even_k(Geo g, CollideParams cp, NativeParams np, typename Store<ST>::T* __restrict__ A,
+              const float* __restrict__ rho_f, const float* __restrict__ u_f, const uint8_t* __restrict__ types) {
+    using R = typename Store<ST>::R;
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    int y, z;
+    row_of<Q>(y, z);
+    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
+    const long long node = g.idx(x, y, z);
+    const uint8_t t = MASK ? __ldg(types + node) : 0;
+    R f[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) f[k] = Store<ST>::ldp(A, k * g.ks + node);
+    uint32_t L = 0;
+    if (MASK) {
+        if (t & kSolid) return;
+        L = links_of<MASK>(t, np.links, node);
+    }
+    R rho;
+    if constexpr (RAW) {
+        // the first collision of a RAW state uses the rho/u fields
+        rho = (R)rho_f[node];
+        const R ux = (R)u_f[node], uy = (R)u_f[g.ks + node], uz = (R)u_f[2 * g.ks + node];
+        const float drho = (ST == 1 || ST == 3) ? __fsub_rn((float)rho, 1.0f) : 0.0f;
+        collide_any<Q, ST, ARITH>(f, rho, ux, uy, uz, drho, cp);
+    } else {
+        update_node<Q, ST, ARITH>(f, rho, cp);
+    }
+    const Nbr nb(g, x, y, z);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        typename Store<ST>::R v = f[k];
+        if (MASK && MOVING && k != 0 && np.moving && ((L >> k) & 1u))
+            v = wall_corrected<Q, ST>(k, v, rho, np.vel[__ldg(types + nb.at<Q>(k, +1)) & kVelMask], np.cs2inv);
+        Store<ST>::st(A, rev_of(k) * g.ks + node, v);
+    }
+}
+
+template <int Q, int ST, bool MASK, int ARITH, bool MOVING>
+__global__ void __launch_bounds__(kBlockX)
+nat_aa_odd_k(Geo g, CollideParams cp, NativeParams np, typename Store<ST>::T* __restrict__ A,
+             const uint8_t* __restrict__ types) {
+    using R = typename Store<ST>::R;
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    int y, z;
+    row_of<Q>(y, z);
+    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
+    const long long node = g.idx(x, y, z);
+    const Nbr nb(g, x, y, z);
+    const uint8_t t = MASK ? __ldg(types + node) : 0;
+    R f[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) f[k] = Store<ST>::ldp(A, rev_of(k) * g.ks + nb.at<Q>(k, -1));
+    uint32_t L = 0;
+    if (MASK) {
+        if (t & kSolid) return;   // (loads issued; a solid node stores nothing)
+        L = links_of<MASK>(t, np.links, node);
+    }
+    if (MASK && L) {
+#pragma unroll
+        for (int k = 1; k < Q; ++k)
+            if ((L >> rev_of(k)) & 1u) f[k] = Store<ST>::ldp(A, k * g.ks + node);
+    }
+    R rho;
+    update_node<Q, ST, ARITH>(f, rho, cp);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        if (MASK && k != 0 && ((L >> k) & 1u)) {
+            typename Store<ST>::R v = f[k];
+            if (MOVING && np.moving)
+                v = wall_corrected<Q, ST>(k, v, rho, np.vel[__ldg(types + nb.at<Q>(k, +1)) & kVelMask], np.cs2inv);
+            Store<ST>::st(A, rev_of(k) * g.ks + node, v);
+        } else {
+            Store<ST>::st(A, k * g.ks + nb.at<Q>(k, +1), f[k]);
+        }
+    }
+}
+
+// Natural populations (storage format, into n_out, may be null) and moments
+// with the solid-node resets (into rho/u, may be null) of an AA buffer in
+// either layout: SWAPPED after an even step, natural after an odd one.
+template <int Q, int ST, bool MASK, bool SWAPPED>
+__global__ void __launch_bounds__(kBlockX)
+nat_aa_gather_k(Geo g, NativeParams np, const typename Store<ST>::T* __restrict__ A,
+                typename Store<ST>::T* __restrict__ n_out, float* __restrict__ rho_f, float* __restrict__ u_f,
+                const uint8_t* __restrict__ types) {
+    using R = typename Store<ST>::R;
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    int y, z;
+    row_of<Q>(y, z);
+    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
+    const long long node = g.idx(x, y, z);
+    uint32_t L = 0;
+    if (MASK) {
+        const uint8_t t = __ldg(types + node);
+        if (t & kSolid) {
+            if (rho_f) {
+                const float* ub = np.vel[t & kVelMask];
+                rho_f[node] = np.rho_solid;
+                u_f[node] = ub[0]; u_f[g.ks + node] = ub[1]; u_f[2 * g.ks + node] = ub[2];
+            }
+            if (n_out) {
+#pragma unroll
+                for (int k = 0; k < Q; ++k)
+                    Store<ST>::st(n_out, k * g.ks + node, (ST == 1 || ST == 3) ? -weight<Q>(k) : (R)0);
+            }
+            return;
+        }
+        L = links_of<MASK>(t, np.links, node);
+    }
+    R f[Q];
+    if constexpr (SWAPPED) {
+        const Nbr nb(g, x, y, z);
+#pragma unroll
+        for (int k = 0; k < Q; ++k) f[k] = Store<ST>::ld(A, rev_of(k) * g.ks + nb.at<Q>(k, -1));
+        if (MASK && L) {
+#pragma unroll
+            for (int k = 1; k < Q; ++k)
+                if ((L >> rev_of(k)) & 1u) f[k] = Store<ST>::ld(A, k * g.ks + node);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < Q; ++k) f[k] = Store<ST>::ld(A, k * g.ks + node);
+    }
+    if (n_out) {
+#pragma unroll
+        for (int k = 0; k < Q; ++k) Store<ST>::st(n_out, k * g.ks + node, f[k]);
+    }
+    if (rho_f) {
+        R rho, ux, uy, uz;
+        moments_any<Q, ST>(f, rho, ux, uy, uz);
+        rho_f[node] = (float)rho;
+        u_f[node] = (float)ux; u_f[g.ks + node] = (float)uy; u_f[2 * g.ks + node] = (float)uz;
+    }
 }
 
 // Gather only: n (storage format) and/or moments, solid nodes reset to
@@ -546,9 +697,10 @@ nat_gather_k(Geo g, NativeParams np, const typename Store<ST>::T* __restrict__ s
              typename Store<ST>::T* __restrict__ n_out, float* __restrict__ rho_f,
              float* __restrict__ u_f, const uint8_t* __restrict__ types) {
     using R = typename Store<ST>::R;
-    const int x = blockIdx.x * kBlockX + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
-    if (x >= g.nx) return;
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    int y, z;
+    row_of<Q>(y, z);
+    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
     const long long node = g.idx(x, y, z);
     uint32_t L = 0;
     if (MASK) {
@@ -562,7 +714,8 @@ nat_gather_k(Geo g, NativeParams np, const typename Store<ST>::T* __restrict__ s
             if (n_out) {
                 // a solid node holds no populations: they read back as 0
 #pragma unroll
-                for (int k = 0; k < Q; ++k) Store<ST>::st(n_out, k * g.ks + node, ST == 1 ? -weight<Q>(k) : (R)0);
+                for (int k = 0; k < Q; ++k)
+                    Store<ST>::st(n_out, k * g.ks + node, (ST == 1 || ST == 3) ? -weight<Q>(k) : (R)0);
             }
             return;
         }
@@ -611,14 +764,15 @@ nat_batch_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks
         const long long node = g.idx(x, y, z);
         const uint8_t* types = D.types;
         const uint8_t tt = __ldg(types + node);
-        if (tt & kSolid) continue;
-        const NativeParams& np = D.np;
-        const uint32_t L = links_of<true>(tt, np.links, node);
         const T* src = static_cast<const T*>(D.f[parity]);
         T* dst = static_cast<T*>(D.f[parity ^ 1]);
         const Nbr nb(g, x, y, z);
         R f[Q];
-        gather_node<Q, ST, true>(src, g, L, nb, node, f);
+        stream_loads<Q, ST>(src, g, nb, f);   // issued with the type load
+        if (tt & kSolid) continue;
+        const NativeParams& np = D.np;
+        const uint32_t L = links_of<true>(tt, np.links, node);
+        bounce_fixup<Q, ST>(src, g, L, node, f);
         R rho;
         update_node<Q, ST, ARITH>(f, rho, D.cp);
         store_node<Q, ST, true, MOVING>(dst, g, np, types, L, nb, node, rho, f);
@@ -631,7 +785,8 @@ template <int Q, int ST, bool MASK, int ARITH>
 int launch_fused(const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
                  const uint8_t* types, cudaStream_t st) {
     using T = typename Store<ST>::T;
-    nat_fused_k<Q, ST, MASK, ARITH><<<cell_grid(g), kBlockX, 0, st>>>(g, cp, np, (const T*)src, (T*)dst, types);
+    nat_fused_k<Q, ST, MASK, ARITH><<<row_grid<Q>(g, 32), dim3(32, kRows), 0, st>>>(g, cp, np, (const T*)src,
+                                                                                    (T*)dst, types);
     return (int)cudaGetLastError();
 }
 
@@ -639,8 +794,8 @@ template <int Q, int ST, bool MASK, int ARITH>
 int launch_raw(const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
                const float* rho, const float* u, const uint8_t* types, cudaStream_t st) {
     using T = typename Store<ST>::T;
-    nat_collide_raw_k<Q, ST, MASK, ARITH><<<cell_grid(g), kBlockX, 0, st>>>(g, cp, np, (const T*)src, (T*)dst,
-                                                                            rho, u, types);
+    nat_collide_raw_k<Q, ST, MASK, ARITH><<<row_grid<Q>(g, 32), dim3(32, kRows), 0, st>>>(
+        g, cp, np, (const T*)src, (T*)dst, rho, u, types);
     return (int)cudaGetLastError();
 }
 
@@ -648,7 +803,8 @@ template <int Q, int ST, bool MASK>
 int launch_gather(const Geo& g, const NativeParams& np, const void* src, void* n_out, float* rho, float* u,
                   const uint8_t* types, cudaStream_t st) {
     using T = typename Store<ST>::T;
-    nat_gather_k<Q, ST, MASK><<<cell_grid(g), kBlockX, 0, st>>>(g, np, (const T*)src, (T*)n_out, rho, u, types);
+    nat_gather_k<Q, ST, MASK><<<row_grid<Q>(g, 32), dim3(32, kRows), 0, st>>>(g, np, (const T*)src, (T*)n_out, rho,
+                                                                              u, types);
     return (int)cudaGetLastError();
 }
 
@@ -663,10 +819,12 @@ auto with_storage_arith(int storage, int arith, F&& f) {
     if constexpr (TRT) {
         if (storage == 1) return f(IC<1>{}, IC<kArithTRT>{});
         if (storage == 2) return f(IC<2>{}, IC<kArithTRT>{});
+        if (storage == 3) return f(IC<3>{}, IC<kArithTRT>{});
         return f(IC<0>{}, IC<kArithTRT>{});
     } else {
         if (storage == 1) return f(IC<1>{}, IC<kArithFP32>{});
         if (storage == 2) return f(IC<2>{}, IC<kArithFP32>{});
+        if (storage == 3) return f(IC<3>{}, IC<kArithFP32>{});
         if (arith == kArithReference) return f(IC<0>{}, IC<kArithReference>{});
         return f(IC<0>{}, IC<kArithFP32>{});
     }
@@ -675,12 +833,13 @@ auto with_storage_arith(int storage, int arith, F&& f) {
 template <int Q, int ARITH, bool MASK>
 int launch_fused_h2(const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
                     const uint8_t* types, cudaStream_t st) {
-    const dim3 grid((g.nx + 2 * kBlockX - 1) / (2 * kBlockX), g.ny, g.nz);
+    const dim3 grid = row_grid<Q>(g, 64);
+    const dim3 block(32, kRows);
     if (MASK && np.moving)
-        nat_fused_h2_k<Q, true, true, ARITH><<<grid, kBlockX, 0, st>>>(g, cp, np, (const __half*)src, (__half*)dst,
+        nat_fused_h2_k<Q, true, true, ARITH><<<grid, block, 0, st>>>(g, cp, np, (const __half*)src, (__half*)dst,
                                                                         types);
     else
-        nat_fused_h2_k<Q, MASK, false, ARITH><<<grid, kBlockX, 0, st>>>(g, cp, np, (const __half*)src, (__half*)dst,
+        nat_fused_h2_k<Q, MASK, false, ARITH><<<grid, block, 0, st>>>(g, cp, np, (const __half*)src, (__half*)dst,
                                                                          types);
     return (int)cudaGetLastError();
 }
@@ -708,6 +867,36 @@ int raw_q(int storage, int arith, bool m, const Geo& g, const CollideParams& cp,
         constexpr int ST = decltype(stc)::value, AR = decltype(arc)::value;
         return m ? launch_raw<Q, ST, true, AR>(g, cp, np, src, dst, rho, u, types, st)
                  : launch_raw<Q, ST, false, AR>(g, cp, np, src, dst, rho, u, types, st);
+    });
+}
+
+// AA steps: kind 0 = even from a RAW state (fields), 1 = even, 2 = odd.
+template <int Q, int ST, bool MASK, int AR>
+int launch_aa(int kind, const Geo& g, const CollideParams& cp, const NativeParams& np, void* A, const float* rho,
+              const float* u, const uint8_t* types, cudaStream_t st) {
+    using T = typename Store<ST>::T;
+    const dim3 grid = row_grid<Q>(g, 32), block(32, kRows);
+    const bool mv = MASK && np.moving;
+    auto go = [&](auto mvc) {
+        constexpr bool MV = decltype(mvc)::value;
+        if (kind == 0)
+            nat_aa_even_k<Q, ST, MASK, AR, MV, true><<<grid, block, 0, st>>>(g, cp, np, (T*)A, rho, u, types);
+        else if (kind == 1)
+            nat_aa_even_k<Q, ST, MASK, AR, MV, false><<<grid, block, 0, st>>>(g, cp, np, (T*)A, rho, u, types);
+        else
+            nat_aa_odd_k<Q, ST, MASK, AR, MV><<<grid, block, 0, st>>>(g, cp, np, (T*)A, types);
+        return (int)cudaGetLastError();
+    };
+    return mv ? go(std::true_type{}) : go(std::false_type{});
+}
+
+template <bool TRT, int Q>
+int aa_q(int kind, int storage, int arith, bool m, const Geo& g, const CollideParams& cp, const NativeParams& np,
+         void* A, const float* rho, const float* u, const uint8_t* types, cudaStream_t st) {
+    return with_storage_arith<TRT>(storage, arith, [&](auto stc, auto arc) {
+        constexpr int ST = decltype(stc)::value, AR = decltype(arc)::value;
+        return m ? launch_aa<Q, ST, true, AR>(kind, g, cp, np, A, rho, u, types, st)
+                 : launch_aa<Q, ST, false, AR>(kind, g, cp, np, A, rho, u, types, st);
     });
 }
 

@@ -258,7 +258,8 @@ void scheduler(plb_server* srv) {
                 finish(srv, r, PLB_REQ_FAILED, e);
                 continue;
             }
-            if (r->p.nx * r->p.ny * r->p.nz >= solo_cells()) {
+            // large solves, and AA ones (batches are AB only), run alone
+            if (r->p.nx * r->p.ny * r->p.nz >= solo_cells() || r->p.streaming == PLB_STREAMING_AA) {
                 auto L = std::make_unique<Lane>();
                 L->solo = true;
                 L->members.push_back(r);
@@ -336,7 +337,8 @@ int64_t plb_solve_bytes(const plb_params* p) {
         ks = round_up(ys * (p->ny + 2) * (p->nz + 2), 64);
     }
     cells_box = (long long)(p->nx + 2) * (p->ny + 2) * (p->nz + 2);
-    long long b = 2LL * p->q * ks * esize;        // two population buffers
+    const long long nbuf = (p->semantics == PLB_SEMANTICS_NATIVE && p->streaming == PLB_STREAMING_AA) ? 1 : 2;
+    long long b = nbuf * p->q * ks * esize;       // population buffers
     b += 4LL * ks * 4;                            // rho, u
     b += 2LL * 27 * 4 + 1024LL * 4 * 8 + 4 * 8;   // constants, reduction partials
     if (p->semantics == PLB_SEMANTICS_NATIVE) b += 2LL * ks + 4LL * ks + cells;   // types, links, mask

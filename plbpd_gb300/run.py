@@ -37,24 +37,27 @@ def params_for(a):
     nx, ny, nz = a.nx or a.n, a.ny or a.n, a.nz or a.n
     if a.model == "D2Q9":
         ny = 1
-    st = capi.STORAGE_FP16_DEV if a.storage == "fp16" else capi.STORAGE_FP32
+    st = {"fp32": capi.STORAGE_FP32, "fp16": capi.STORAGE_FP16_DEV, "fp32dev": capi.STORAGE_FP32_DEV,
+          "fp64": capi.STORAGE_FP64}[a.storage]
     ar = capi.ARITH_REFERENCE if a.arith == "reference" else capi.ARITH_FP32
+    col = dict(collision=capi.COLLISION_TRT if a.collision == "trt" else capi.COLLISION_BGK)
     nu = nu_for_tau(a.tau)
     if a.workload == "periodic":
         faces = {f: "periodic" for f in capi.FACES}
         return capi.make_params(a.model, nx, ny, nz, nu, face_type=faces, u0=(0.01, 0.0, 0.0),
-                                semantics=capi.SEMANTICS_NATIVE, arith=ar, storage=st)
+                                semantics=capi.SEMANTICS_NATIVE, arith=ar, storage=st, **col)
     if a.workload == "duct":
-        faces = {"east": "periodic", "west": "periodic", "north": "noslip", "south": "noslip", "up": "noslip",
-                 "down": "noslip"}
-        vel = {f: (0.0, 0.0, 0.0) for f in ("north", "south", "up", "down")}
+        # D2Q9 moves in x-z only: its channel has walls up and down
+        walls = ("up", "down") if a.model == "D2Q9" else ("north", "south", "up", "down")
+        faces = {"east": "periodic", "west": "periodic", **{f: "noslip" for f in walls}}
+        vel = {f: (0.0, 0.0, 0.0) for f in walls}
         return capi.make_params(a.model, nx, ny, nz, nu, force=(a.force, 0.0, 0.0), face_type=faces, face_vel=vel,
-                                semantics=capi.SEMANTICS_NATIVE, arith=ar, storage=st)
+                                semantics=capi.SEMANTICS_NATIVE, arith=ar, storage=st, **col)
     if a.workload == "channel":
         faces = {"east": "periodic", "west": "periodic", "up": "noslip", "down": "noslip"}
         vel = {"up": (0.0, 0.0, 0.0), "down": (0.0, 0.0, 0.0)}
         return capi.make_params(a.model, nx, ny, nz, nu, force=(a.force, 0.0, 0.0), face_type=faces, face_vel=vel,
-                                semantics=capi.SEMANTICS_REFERENCE, arith=ar)
+                                semantics=capi.SEMANTICS_REFERENCE, arith=ar, **col)
     raise SystemExit(f"unknown workload {a.workload}")
 
 
@@ -71,7 +74,8 @@ def main(argv=None):
     ap.add_argument("--spheres", action="store_true")
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16"])
+    ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16", "fp32dev", "fp64"])
+    ap.add_argument("--collision", default="bgk", choices=["bgk", "trt"])
     ap.add_argument("--arith", default="fp32", choices=["fp32", "reference"])
     a = ap.parse_args(argv)
     p = params_for(a)

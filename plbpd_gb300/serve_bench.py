@@ -4,7 +4,7 @@
 
 Requests (seeded): Poisson arrivals at --rate per second; 60% D2Q9 with a
 square grid of edge log-uniform in [64, 2048], 40% D3Q19 with a cube of edge
-log-uniform in [32, 160]; FP32 or FP16 storage 50/50; tau uniform in
+log-uniform in [32, 160]; FP32 (f - w by default) or FP16 storage 50/50; tau uniform in
 [0.55, 1.5]; random 2x2x2 obstacles at 0-20% solid; 500-5000 steps; periodic
 x, resting walls on the other moving axes, a body force.  The server admits
 by device bytes under --budget-gb.  Printed: solves/s and p50/p99 latency
@@ -54,8 +54,12 @@ def make_requests(n: int, rate: float, seed: int, min_steps: int = 500, max_step
     return out
 
 
+FP32_STORAGE = {"dev": capi.STORAGE_FP32_DEV, "plain": capi.STORAGE_FP32}
+_fp32 = [capi.STORAGE_FP32_DEV]
+
+
 def params_of(r, storage=None):
-    st = storage if storage is not None else (capi.STORAGE_FP16_DEV if r["fp16"] else capi.STORAGE_FP32)
+    st = storage if storage is not None else (capi.STORAGE_FP16_DEV if r["fp16"] else _fp32[0])
     nx, ny, nz = r["dims"]
     return capi.make_params(r["model"], nx, ny, nz, r["nu"], force=(r["force"], 0.0, 0.0), face_type=r["faces"],
                             face_vel=r["vel"], semantics=capi.SEMANTICS_NATIVE, arith=capi.ARITH_FP32, storage=st)
@@ -86,7 +90,10 @@ def main(argv=None):
     ap.add_argument("--plain", type=int, default=-1, help="requests run as serial plain solves (default: all)")
     ap.add_argument("--accuracy-sample", type=int, default=6)
     ap.add_argument("--max-steps", type=int, default=5000)
+    ap.add_argument("--fp32-storage", choices=sorted(FP32_STORAGE), default="dev",
+                    help="storage of the FP32 half: f - w (dev) or f (plain, plbpd's)")
     a = ap.parse_args(argv)
+    _fp32[0] = FP32_STORAGE[a.fp32_storage]
     reqs = make_requests(a.requests, a.rate, a.seed, max_steps=a.max_steps)
     masks = [mask_of(r) for r in reqs]
     cell_updates = sum(np.prod(r["dims"]) * r["steps"] for r in reqs)
@@ -136,7 +143,7 @@ def main(argv=None):
 
     served_rate = len(reqs) / t_served
     print(json.dumps({
-        "workload": "served stream", "requests": len(reqs), "arrival_rate": a.rate,
+        "workload": "served stream", "requests": len(reqs), "arrival_rate": a.rate, "fp32_storage": a.fp32_storage,
         "cell_updates": float(cell_updates), "served_seconds": round(t_served, 2),
         "served_solves_per_s": round(served_rate, 3), "served_mlups": round(cell_updates / t_served / 1e6, 1),
         "latency_p50_s": round(float(np.percentile(lats, 50)), 3),

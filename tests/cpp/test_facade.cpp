@@ -26,6 +26,7 @@
 
 #include "Boundary.hpp"
 #include "CalcMoments.hpp"
+#include "CollisionTRT.hpp"
 #include "Domain.hpp"
 #include "EqlbDist.hpp"
 #include "Field.hpp"
@@ -119,6 +120,8 @@ static int run_cpu() {
         expect_throw<std::logic_error>([&] { st(sd, "sideways"); }, "bad stream type");
         expect_throw<std::logic_error>([&] { st(sd, "pull"); }, "pull streaming");
         expect_throw<std::logic_error>([&] { st(sd, "pull", true); }, "pull streaming (reference)");
+        Domain d(&m, 4, 1, 3, 0.1f, 1.0f, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f});
+        expect_throw<std::invalid_argument>([&] { CollisionTRT c(&m, &d, -1.0f); }, "negative TRT magic");
     }
     // tables and the TestEqlbDist known answer, for the Python side
     std::printf("{");
@@ -207,6 +210,24 @@ static int run_case(int argc, char** argv) {
     SimData back(domain->get_dimensions(), lbmodel->get_num_directions());
     back.read_state(dir + "/state.plb");
     for (size_t i = 0; i < simdata.n->size(); ++i) CHECK(back.n->get(0, 0, 0, 0)[i] == simdata.n->get(0, 0, 0, 0)[i]);
+    // a hand-written loop with the second Collision subclass in place of
+    // CollisionSRT: 6 steps of collide, push, no-slip, periodicity, moments, reset
+    {
+        auto trt_data = SimData(domain->get_dimensions(), lbmodel->get_num_directions());
+        problem->initialize(trt_data);
+        const std::unique_ptr<Collision> collide = std::make_unique<CollisionTRT>(lbmodel.get(), domain.get());
+        CHECK(static_cast<const CollisionTRT&>(*collide).get_magic() == 3.0f / 16.0f);
+        Streaming stream(lbmodel.get());
+        for (int t = 0; t < 6; ++t) {
+            (*collide)(trt_data, false);
+            stream(trt_data, "push");
+            boundary->apply_noslip(trt_data);
+            boundary->apply_periodicity(trt_data);
+            moments(trt_data);
+            boundary->reset(trt_data);
+        }
+        dump_all(dir, "trt6", trt_data);
+    }
     problem->print_times();
     return 0;
 }

@@ -81,6 +81,23 @@ def test_facade_matches_reference(exe, tmp_path, case):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("case", ["d2q9_channel", "d3q19_xy_periodic", "d3q27_duct"])
+def test_facade_collision_trt_matches_oracle(exe, tmp_path, case):
+    """CollisionTRT through the Collision base in a hand-written plbpd loop
+    equals the oracle's REFERENCE-mode run with the TRT operator."""
+    import pyoracle as po
+    cfg = CASES[case]
+    r = subprocess.run([exe, "case", str(tmp_path)] + case_args(cfg), capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    p = po.Port(**cfg, arith=po.ARITH_FP32, trt=0.0)
+    p.initialize()
+    p.step(6)
+    for fld, w in (("n", po.N), ("rho", po.RHO), ("u", po.U)):
+        want = p.get(w)
+        assert_bitexact(read_f32(tmp_path / f"trt6_{fld}.f32", want.shape), want, f"{case} TRT {fld}")
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("preset", sorted(PRESETS))
 def test_facade_flow_presets_match_reference(exe, tmp_path, golden, preset):
     """src/main.cpp's flow -- Flow, PLBPD, SimData, initialize, march_in_time

@@ -34,11 +34,11 @@ def make_solves(capi, storage, seed=5, count=7, model="D3Q19"):
     return out
 
 
-@pytest.mark.parametrize("storage_name", ["fp32", "fp16"])
+@pytest.mark.parametrize("storage_name", ["fp32", "fp16", "fp32dev"])
 @pytest.mark.parametrize("model", ["D3Q19", "D3Q27"])
 def test_batch_equals_each_domain_alone(storage_name, model):
     from plbpd_gb300 import capi
-    storage = capi.STORAGE_FP32 if storage_name == "fp32" else capi.STORAGE_FP16_DEV
+    storage = {"fp32": capi.STORAGE_FP32, "fp16": capi.STORAGE_FP16_DEV, "fp32dev": capi.STORAGE_FP32_DEV}[storage_name]
     mix = make_solves(capi, storage, model=model)
     alone = make_solves(capi, storage, model=model)
     with capi.Batch(mix) as b:

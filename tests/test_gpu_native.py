@@ -85,7 +85,7 @@ def p_face_solid(p):
     return solid
 
 
-@pytest.mark.parametrize("arith", ["fp32", "reference", "fp16", "fp64"])
+@pytest.mark.parametrize("arith", ["fp32", "reference", "fp16", "fp64", "fp32dev"])
 @pytest.mark.parametrize("case", sorted(NATIVE_CASES))
 def test_native_matches_oracle(case, arith):
     """FP32 storage with either arithmetic, FP16 deviation storage and FP64
@@ -94,9 +94,11 @@ def test_native_matches_oracle(case, arith):
     cfg = NATIVE_CASES[case]
     mask = mask_for(case, cfg)
     port_kw = {"fp32": dict(arith=po.ARITH_FP32), "reference": dict(arith=po.ARITH_AVX2),
-               "fp16": dict(arith=po.ARITH_FP16DEV), "fp64": dict(precision=1)}[arith]
+               "fp16": dict(arith=po.ARITH_FP16DEV), "fp64": dict(precision=1),
+               "fp32dev": dict(arith=po.ARITH_FP32DEV)}[arith]
     gpu_kw = {"fp32": dict(arith=capi.ARITH_FP32), "reference": dict(arith=capi.ARITH_REFERENCE),
-              "fp16": dict(storage=capi.STORAGE_FP16_DEV), "fp64": dict(storage=capi.STORAGE_FP64)}[arith]
+              "fp16": dict(storage=capi.STORAGE_FP16_DEV), "fp64": dict(storage=capi.STORAGE_FP64),
+              "fp32dev": dict(storage=capi.STORAGE_FP32_DEV)}[arith]
     p = po.Port(**cfg, mode=po.MODE_NATIVE, mask=mask, **port_kw)
     p._cfg = cfg
     p.initialize()
@@ -150,3 +152,24 @@ def test_fp16_storage_tracks_fp64_oracle(case):
         r64 = d.get64(po.RHO)[1:-1, 1:-1, 1:-1]
         assert rel_l2(u16, u64) < 2e-2, rel_l2(u16, u64)
         assert rel_l2(r16, r64) < 1e-4, rel_l2(r16, r64)
+
+
+def test_fp32_deviation_storage_accuracy():
+    """A slow flow (u ~ 1e-5): FP32 storage of f loses most digits of u to the
+    rounding of f ~ w, FP32 storage of f - w keeps them."""
+    from plbpd_gb300 import capi
+    cfg = dict(NATIVE_CASES["obstacles_d3q19"], force=(1e-7, 0.0, 0.0))
+    mask = mask_for("obstacles_d3q19", cfg)
+    d = po.Port(**cfg, mode=po.MODE_NATIVE, precision=1, mask=mask)
+    d.initialize()
+    d.step(300)
+    u64 = d.get64(po.U)[1:-1, 1:-1, 1:-1]
+    err = {}
+    for name, st in (("fp32", capi.STORAGE_FP32), ("fp32dev", capi.STORAGE_FP32_DEV)):
+        with capi.Solve.create(**cfg, semantics=capi.SEMANTICS_NATIVE, arith=capi.ARITH_FP32, storage=st) as s:
+            s.set_mask(mask)
+            s.initialize()
+            s.step(300)
+            err[name] = rel_l2(s.get(3)[1:-1, 1:-1, 1:-1], u64)
+    assert err["fp32dev"] < 1e-4, err
+    assert err["fp32dev"] < err["fp32"] / 10, err

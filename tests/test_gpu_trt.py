@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 import pyoracle as po
+from conftest import assert_bitexact
 from test_gpu_native import NATIVE_CASES, compare, mask_for, perturbed_start
 
 pytestmark = pytest.mark.gpu
@@ -16,16 +17,17 @@ MAGIC = {"channel_d2q9": 0.0, "duct_d3q27": 0.25, "obstacles_d3q19": 0.0, "torus
          "torus_d3q27": 0.0}
 
 
-@pytest.mark.parametrize("storage", ["fp32", "fp16", "fp64"])
+@pytest.mark.parametrize("storage", ["fp32", "fp16", "fp64", "fp32dev"])
 @pytest.mark.parametrize("case", CASES)
 def test_trt_matches_oracle(case, storage):
     from plbpd_gb300 import capi
     cfg = NATIVE_CASES[case]
     mask = mask_for(case, cfg)
     port_kw = {"fp32": dict(arith=po.ARITH_FP32), "fp16": dict(arith=po.ARITH_FP16DEV),
-               "fp64": dict(precision=1)}[storage]
+               "fp64": dict(precision=1), "fp32dev": dict(arith=po.ARITH_FP32DEV)}[storage]
     gpu_kw = {"fp32": dict(arith=capi.ARITH_FP32), "fp16": dict(storage=capi.STORAGE_FP16_DEV, arith=capi.ARITH_FP32),
-              "fp64": dict(storage=capi.STORAGE_FP64, arith=capi.ARITH_FP32)}[storage]
+              "fp64": dict(storage=capi.STORAGE_FP64, arith=capi.ARITH_FP32),
+              "fp32dev": dict(storage=capi.STORAGE_FP32_DEV, arith=capi.ARITH_FP32)}[storage]
     p = po.Port(**cfg, mode=po.MODE_NATIVE, mask=mask, trt=MAGIC[case], **port_kw)
     p._cfg = cfg
     p.initialize()
@@ -44,6 +46,42 @@ def test_trt_matches_oracle(case, storage):
             done = target
             compare(s, p, mask, f"TRT {case} {storage} step {target}")
         np.testing.assert_allclose(s.conservation(), p.conservation(), rtol=1e-11, atol=1e-12)
+
+
+@pytest.mark.parametrize("case", sorted(["d2q9_channel", "d3q19_xy_periodic"]))
+def test_trt_reference_semantics_matches_oracle(case):
+    """plbpd's operator sequence (push streaming, serial no-slip, halo
+    periodicity) with the TRT collision, fused and operator by operator."""
+    from cases import CASES
+    from plbpd_gb300 import capi
+    cfg = CASES[case]
+    p = po.Port(**cfg, arith=po.ARITH_FP32, trt=0.0)
+    p.initialize()
+    with capi.Solve.create(**cfg, collision=capi.COLLISION_TRT) as s:
+        s.initialize()
+        done = 0
+        for target in (1, 6, 40):
+            p.step(target - done)
+            s.step(target - done)
+            done = target
+            for name, w in (("n", 0), ("ntmp", 1), ("rho", 2), ("u", 3)):
+                assert_bitexact(s.get(w), p.get(w), f"TRT {case} step {target} {name}")
+        s.collide(); p.collide()
+        assert_bitexact(s.get(0), p.get(0), f"TRT {case} collide")
+
+
+def test_set_collision_switches_operator():
+    from cases import CASES
+    from plbpd_gb300 import capi
+    cfg = CASES["d2q9_channel"]
+    p = po.Port(**cfg, arith=po.ARITH_FP32, trt=0.25)
+    p.initialize()
+    with capi.Solve.create(**cfg) as s:
+        s.set_collision(capi.COLLISION_TRT, 0.25)
+        s.initialize()
+        p.step(9)
+        s.step(9)
+        assert_bitexact(s.get(0), p.get(0), "TRT after plb_set_collision")
 
 
 def test_trt_poiseuille_on_gpu():
@@ -103,11 +141,8 @@ def test_trt_refused_where_undefined():
     from plbpd_gb300 import capi
     faces = {"east": "periodic", "west": "periodic", "up": "noslip", "down": "noslip"}
     vel = {"up": (0, 0, 0), "down": (0, 0, 0)}
-    with pytest.raises(capi.PlbError):      # REFERENCE semantics reproduce plbpd's BGK
-        capi.Solve.create("D2Q9", 8, 1, 6, 0.1, face_type=faces, face_vel=vel, collision=capi.COLLISION_TRT)
-    with pytest.raises(capi.PlbError):      # plbpd's arithmetic is BGK's
-        capi.Solve.create("D2Q9", 8, 1, 6, 0.1, face_type=faces, face_vel=vel, semantics=capi.SEMANTICS_NATIVE,
-                          arith=capi.ARITH_REFERENCE, collision=capi.COLLISION_TRT)
+    with pytest.raises(capi.PlbError):      # no such operator
+        capi.Solve.create("D2Q9", 8, 1, 6, 0.1, face_type=faces, face_vel=vel, collision=7)
     with pytest.raises(capi.PlbError):      # tau must exceed 1/2
         capi.Solve.create("D2Q9", 8, 1, 6, 0.0, face_type=faces, face_vel=vel, semantics=capi.SEMANTICS_NATIVE,
                           arith=capi.ARITH_FP32, collision=capi.COLLISION_TRT)

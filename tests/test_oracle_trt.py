@@ -47,8 +47,9 @@ def test_trt_rejected_where_undefined():
     with pytest.raises(ValueError):   # plbpd's own arithmetic is BGK only
         po.Port("D2Q9", 4, 1, 6, 0.1, 1.0, (0, 0, 0), (0, 0, 0), 1.0, CHANNEL, STILL, mode=po.MODE_NATIVE,
                 arith=po.ARITH_AVX2, trt=0.0)
-    with pytest.raises(ValueError):   # REFERENCE mode reproduces plbpd's BGK
-        po.Port("D2Q9", 4, 1, 6, 0.1, 1.0, (0, 0, 0), (0, 0, 0), 1.0, CHANNEL, STILL, trt=0.0)
+    with pytest.raises(ValueError):   # tau must exceed 1/2
+        po.Port("D2Q9", 4, 1, 6, 0.0, 1.0, (0, 0, 0), (0, 0, 0), 1.0, CHANNEL, STILL, mode=po.MODE_NATIVE,
+                arith=po.ARITH_FP32, trt=0.0)
 
 
 def test_trt_conserves_mass_and_momentum_without_force():
