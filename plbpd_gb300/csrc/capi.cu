@@ -807,10 +807,11 @@ int plb_get_field(plb_solve* s, int32_t which, float* out) {
     if (s->native) {
         if (which == PLB_FIELD_NTMP) { std::memset(out, 0, len * sizeof(float)); return PLB_OK; }
         if (s->post && s->aa) {
-            if (which == PLB_FIELD_N && s->swapped) {
+            if (which == PLB_FIELD_N) {
+                // also from the natural layout: the gather reads solid nodes as 0, as the two-buffer path does
                 PLB_CUDA(cudaMallocAsync(&tmp, pop_bytes(s), s->stream));
-                const int e = nat_aa_gather(s->q, s->storage, s->has_mask, true, s->g, s->np, s->f[0], tmp, nullptr,
-                                            nullptr, s->types, s->stream);
+                const int e = nat_aa_gather(s->q, s->storage, s->has_mask, s->swapped, s->g, s->np, s->f[0], tmp,
+                                            nullptr, nullptr, s->types, s->stream);
                 if (e != 0) {
                     cudaFreeAsync(tmp, s->stream);
                     return fail(PLB_ECUDA, std::string("nat_aa_gather: ") + cudaGetErrorString((cudaError_t)e));

@@ -142,9 +142,8 @@ template <int Q, int ST>
 int aa_gather_st(bool m, bool swapped, const Geo& g, const NativeParams& np, const void* A, void* n_out, float* rho,
                  float* u, const uint8_t* types, cudaStream_t st) {
     using T = typename Store<ST>::T;
-    const dim3 grid = row_grid<Q>(g, 32), block(32, kRows);
     auto go = [&](auto mc, auto sc) {
-        nat_aa_gather_k<Q, ST, decltype(mc)::value, decltype(sc)::value><<<grid, block, 0, st>>>(
+        nat_aa_gather_k<Q, ST, decltype(mc)::value, decltype(sc)::value><<<cell_grid(g), kBlockX, 0, st>>>(
             g, np, (const T*)A, (T*)n_out, rho, u, types);
         return (int)cudaGetLastError();
     };

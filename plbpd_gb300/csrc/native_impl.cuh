@@ -32,23 +32,19 @@ namespace {
 
 constexpr int kBlockX = 128;
 
-// Thread blocks of the per-node kernels are 32 x kRows: each warp takes 32
-// consecutive x (64 for the FP16 pair kernel) of one row, so a row of any
-// length leaves at most one warp partly idle.  Rows run along y for the 3-D
-// lattices and along z for D2Q9, whose domains are one node thick in y.
-constexpr int kRows = kBlockX / 32;
-
-template <int Q>
-__device__ __forceinline__ void row_of(int& y, int& z) {
-    if (Q == 9) { y = blockIdx.y; z = blockIdx.z * kRows + threadIdx.y; }
-    else { y = blockIdx.y * kRows + threadIdx.y; z = blockIdx.z; }
+// Thread blocks of the hot per-node kernels are one segment of a row: 4 warps
+// along x (128 threads) when the row is a whole number of such blocks long,
+// else one warp, so a row of any length leaves at most one warp partly idle.
+// The row (y, z) comes from the block index alone, which keeps the row
+// offsets warp-uniform (they live in uniform registers); a thread index in
+// them costs registers and occupancy.  BX is the block width.
+inline int block_x(const Geo& g, int nodes_per_thread) {
+    return g.nx % (kBlockX * nodes_per_thread) == 0 ? kBlockX : 32;
 }
 
-template <int Q>
-dim3 row_grid(const Geo& g, int x_per_warp) {
-    const unsigned gx = (unsigned)((g.nx + x_per_warp - 1) / x_per_warp);
-    return Q == 9 ? dim3(gx, (unsigned)g.ny, (unsigned)((g.nz + kRows - 1) / kRows))
-                  : dim3(gx, (unsigned)((g.ny + kRows - 1) / kRows), (unsigned)g.nz);
+inline dim3 seg_grid(const Geo& g, int bx, int nodes_per_thread) {
+    const long long xs = (long long)bx * nodes_per_thread;
+    return dim3((unsigned)((g.nx + xs - 1) / xs), (unsigned)g.ny, (unsigned)g.nz);
 }
 
 // Storage accessors: ld reads through the read-only path (buffers the kernel
@@ -88,18 +84,17 @@ template <> struct Store<2> {
 
 // Neighbour index helper: element offsets of x-1, x, x+1 (and y, z) with the
 // periodic axes wrapped.  A fluid node never has a neighbour outside the box
-// along a walled axis, because the wall layer in between is solid; for the
-// wall layer itself such a neighbour is clamped to the node's own row, so
-// that kernels may load a node's sources before they know it is solid.
+// along a walled axis, because the wall layer in between is solid, so kernels
+// index a node's neighbours only after they know it is fluid.
 struct Nbr {
     long long xo[3], yo[3], zo[3];
     __device__ __forceinline__ Nbr(const Geo& g, int x, int y, int z) {
-        const int xm = x == 0 ? (g.wrap_x ? g.nx - 1 : x) : x - 1;
-        const int xp = x == g.nx - 1 ? (g.wrap_x ? 0 : x) : x + 1;
-        const int ym = y == 0 ? (g.wrap_y ? g.ny - 1 : y) : y - 1;
-        const int yp = y == g.ny - 1 ? (g.wrap_y ? 0 : y) : y + 1;
-        const int zm = z == 0 ? (g.wrap_z ? g.nz - 1 : z) : z - 1;
-        const int zp = z == g.nz - 1 ? (g.wrap_z ? 0 : z) : z + 1;
+        const int xm = (x == 0 && g.wrap_x) ? g.nx - 1 : x - 1;
+        const int xp = (x == g.nx - 1 && g.wrap_x) ? 0 : x + 1;
+        const int ym = (y == 0 && g.wrap_y) ? g.ny - 1 : y - 1;
+        const int yp = (y == g.ny - 1 && g.wrap_y) ? 0 : y + 1;
+        const int zm = (z == 0 && g.wrap_z) ? g.nz - 1 : z - 1;
+        const int zp = (z == g.nz - 1 && g.wrap_z) ? 0 : z + 1;
         xo[0] = xm + g.xoff; xo[1] = x + g.xoff; xo[2] = xp + g.xoff;
         yo[0] = (long long)ym * g.ys; yo[1] = (long long)y * g.ys; yo[2] = (long long)yp * g.ys;
         zo[0] = (long long)zm * g.zs; zo[1] = (long long)z * g.zs; zo[2] = (long long)zp * g.zs;
@@ -344,12 +339,11 @@ __device__ __forceinline__ uint32_t links_of(const uint8_t t, const uint32_t* __
     return (MASK && (t & kNearSolid)) ? __ldg(links + node) : 0u;
 }
 
-// Gathers n[x][*] from P: the streaming loads, then the bounce-back fix-up.
-// Every source address is inside the box (a solid source is a node too, and
-// Nbr clamps at walled faces), so the streaming loads are unconditional and
-// are issued before the node's type is known; bounce-back directions are then
-// replaced by the node's own reversed slot.  `links` bit k is set when
-// x + c_k is solid, so the source x - c_k is solid when bit rev(k) is.
+// Gathers n[x][*] from P for a fluid node: the streaming loads, then the
+// bounce-back fix-up.  Every source is inside the box (a solid source is a
+// node too), so the streaming loads are unconditional; bounce-back directions
+// are then replaced by the node's own reversed slot.  `links` bit k is set
+// when x + c_k is solid, so the source x - c_k is solid when bit rev(k) is.
 template <int Q, int ST>
 __device__ __forceinline__ void stream_loads(const typename Store<ST>::T* __restrict__ src, const Geo& g,
                                              const Nbr& nb, typename Store<ST>::R (&f)[Q]) {
@@ -376,28 +370,27 @@ __device__ __forceinline__ void gather_node(const typename Store<ST>::T* __restr
 }
 
 // ---------------------------------------------------------------------------
-template <int Q, int ST, bool MASK, int ARITH>
-__global__ void __launch_bounds__(kBlockX)
+template <int Q, int ST, bool MASK, int ARITH, int BX>
+__global__ void __launch_bounds__(BX)
 nat_fused_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::T* __restrict__ src,
             typename Store<ST>::T* __restrict__ dst, const uint8_t* __restrict__ types) {
     using R = typename Store<ST>::R;
-    const int x = blockIdx.x * 32 + threadIdx.x;
-    int y, z;
-    row_of<Q>(y, z);
-    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
+    const int x = blockIdx.x * BX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
     const long long node = g.idx(x, y, z);
-    const Nbr nb(g, x, y, z);
-    // the type and the streaming loads are issued together: waiting for the
-    // type first would add a memory round trip before the loads
-    const uint8_t t = MASK ? __ldg(types + node) : 0;
-    R f[Q];
-    stream_loads<Q, ST>(src, g, nb, f);
+    // the type is read first: loading a solid node's sources would cost
+    // traffic in obstacle-filled regions (measured 15% slower on D3Q27 with
+    // 15% solid spheres), more than the round trip it saves
     uint32_t L = 0;
     if (MASK) {
+        const uint8_t t = __ldg(types + node);
         if (t & kSolid) return;
         L = links_of<MASK>(t, np.links, node);
-        bounce_fixup<Q, ST>(src, g, L, node, f);
     }
+    const Nbr nb(g, x, y, z);
+    R f[Q];
+    gather_node<Q, ST, MASK>(src, g, L, nb, node, f);
     R rho;
     update_node<Q, ST, ARITH>(f, rho, cp);
     store_node<Q, ST, MASK>(dst, g, np, types, L, nb, node, rho, f);
@@ -420,16 +413,14 @@ nat_fused_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::
 // and measured 1.6x (D3Q19) to 2.3x (D3Q27) slower.  A source row outside a
 // walled axis only occurs for pairs in a wall row, which are solid and store
 // nothing; its address is clamped to the pair's own row.
-template <int Q, bool MASK, bool MOVING, int ARITH>
-__global__ void __launch_bounds__(kBlockX)
+template <int Q, bool MASK, bool MOVING, int ARITH, int BX>
+__global__ void __launch_bounds__(BX)
 nat_fused_h2_k(Geo g, CollideParams cp, NativeParams np, const __half* __restrict__ src, __half* __restrict__ dst,
                const uint8_t* __restrict__ types) {
     const unsigned kFull = 0xffffffffu;
-    const int lane = threadIdx.x;   // blockDim.x is 32: a warp is one row
-    const int x0 = 2 * (blockIdx.x * 32 + threadIdx.x);
-    int y, z;
-    row_of<Q>(y, z);
-    if (y >= g.ny || z >= g.nz) return;   // the whole warp: no shuffle is left half done
+    const int lane = threadIdx.x & 31;   // a warp is 32 consecutive pairs of one row
+    const int x0 = 2 * (blockIdx.x * BX + threadIdx.x);
+    const int y = blockIdx.y, z = blockIdx.z;
     const bool active = x0 < g.nx;
     const int ym = y == 0 ? (g.wrap_y ? g.ny - 1 : y) : y - 1;
     const int yp = y == g.ny - 1 ? (g.wrap_y ? 0 : y) : y + 1;
@@ -520,10 +511,9 @@ nat_collide_raw_k(Geo g, CollideParams cp, NativeParams np, const typename Store
                   typename Store<ST>::T* __restrict__ dst, const float* __restrict__ rho_f,
                   const float* __restrict__ u_f, const uint8_t* __restrict__ types) {
     using R = typename Store<ST>::R;
-    const int x = blockIdx.x * 32 + threadIdx.x;
-    int y, z;
-    row_of<Q>(y, z);
-    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
+    const int x = blockIdx.x * kBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
     const long long node = g.idx(x, y, z);
     uint32_t L = 0;
     if (MASK) {
@@ -552,25 +542,24 @@ nat_collide_raw_k(Geo g, CollideParams cp, NativeParams np, const typename Store
 // odd step A holds the pre-collision populations in the natural layout.
 // Bounce-back values carry the moving-wall term when stored.  Every value is
 // the one the two-buffer kernel computes, so the two are bit-identical.
-template <int Q, int ST, bool MASK, int ARITH, bool MOVING, bool RAW>
-__global__ void __launch_bounds__(kBlockX)
+template <int Q, int ST, bool MASK, int ARITH, bool MOVING, bool RAW, int BX>
+__global__ void __launch_bounds__(BX)
 nat_aa_even_k(Geo g, CollideParams cp, NativeParams np, typename Store<ST>::T* __restrict__ A,
               const float* __restrict__ rho_f, const float* __restrict__ u_f, const uint8_t* __restrict__ types) {
     using R = typename Store<ST>::R;
-    const int x = blockIdx.x * 32 + threadIdx.x;
-    int y, z;
-    row_of<Q>(y, z);
-    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
+    const int x = blockIdx.x * BX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
     const long long node = g.idx(x, y, z);
-    const uint8_t t = MASK ? __ldg(types + node) : 0;
-    R f[Q];
-#pragma unroll
-    for (int k = 0; k < Q; ++k) f[k] = Store<ST>::ldp(A, k * g.ks + node);
     uint32_t L = 0;
     if (MASK) {
+        const uint8_t t = __ldg(types + node);
         if (t & kSolid) return;
         L = links_of<MASK>(t, np.links, node);
     }
+    R f[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) f[k] = Store<ST>::ldp(A, k * g.ks + node);
     R rho;
     if constexpr (RAW) {
         // the first collision of a RAW state uses the rho/u fields
@@ -591,26 +580,25 @@ nat_aa_even_k(Geo g, CollideParams cp, NativeParams np, typename Store<ST>::T* _
     }
 }
 
-template <int Q, int ST, bool MASK, int ARITH, bool MOVING>
-__global__ void __launch_bounds__(kBlockX)
+template <int Q, int ST, bool MASK, int ARITH, bool MOVING, int BX>
+__global__ void __launch_bounds__(BX)
 nat_aa_odd_k(Geo g, CollideParams cp, NativeParams np, typename Store<ST>::T* __restrict__ A,
              const uint8_t* __restrict__ types) {
     using R = typename Store<ST>::R;
-    const int x = blockIdx.x * 32 + threadIdx.x;
-    int y, z;
-    row_of<Q>(y, z);
-    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
+    const int x = blockIdx.x * BX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
     const long long node = g.idx(x, y, z);
+    uint32_t L = 0;
+    if (MASK) {
+        const uint8_t t = __ldg(types + node);
+        if (t & kSolid) return;
+        L = links_of<MASK>(t, np.links, node);
+    }
     const Nbr nb(g, x, y, z);
-    const uint8_t t = MASK ? __ldg(types + node) : 0;
     R f[Q];
 #pragma unroll
     for (int k = 0; k < Q; ++k) f[k] = Store<ST>::ldp(A, rev_of(k) * g.ks + nb.at<Q>(k, -1));
-    uint32_t L = 0;
-    if (MASK) {
-        if (t & kSolid) return;   // (loads issued; a solid node stores nothing)
-        L = links_of<MASK>(t, np.links, node);
-    }
     if (MASK && L) {
 #pragma unroll
         for (int k = 1; k < Q; ++k)
@@ -640,10 +628,9 @@ nat_aa_gather_k(Geo g, NativeParams np, const typename Store<ST>::T* __restrict_
                 typename Store<ST>::T* __restrict__ n_out, float* __restrict__ rho_f, float* __restrict__ u_f,
                 const uint8_t* __restrict__ types) {
     using R = typename Store<ST>::R;
-    const int x = blockIdx.x * 32 + threadIdx.x;
-    int y, z;
-    row_of<Q>(y, z);
-    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
+    const int x = blockIdx.x * kBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
     const long long node = g.idx(x, y, z);
     uint32_t L = 0;
     if (MASK) {
@@ -697,10 +684,9 @@ nat_gather_k(Geo g, NativeParams np, const typename Store<ST>::T* __restrict__ s
              typename Store<ST>::T* __restrict__ n_out, float* __restrict__ rho_f,
              float* __restrict__ u_f, const uint8_t* __restrict__ types) {
     using R = typename Store<ST>::R;
-    const int x = blockIdx.x * 32 + threadIdx.x;
-    int y, z;
-    row_of<Q>(y, z);
-    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
+    const int x = blockIdx.x * kBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
     const long long node = g.idx(x, y, z);
     uint32_t L = 0;
     if (MASK) {
@@ -764,15 +750,14 @@ nat_batch_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks
         const long long node = g.idx(x, y, z);
         const uint8_t* types = D.types;
         const uint8_t tt = __ldg(types + node);
+        if (tt & kSolid) continue;
+        const NativeParams& np = D.np;
+        const uint32_t L = links_of<true>(tt, np.links, node);
         const T* src = static_cast<const T*>(D.f[parity]);
         T* dst = static_cast<T*>(D.f[parity ^ 1]);
         const Nbr nb(g, x, y, z);
         R f[Q];
-        stream_loads<Q, ST>(src, g, nb, f);   // issued with the type load
-        if (tt & kSolid) continue;
-        const NativeParams& np = D.np;
-        const uint32_t L = links_of<true>(tt, np.links, node);
-        bounce_fixup<Q, ST>(src, g, L, node, f);
+        gather_node<Q, ST, true>(src, g, L, nb, node, f);
         R rho;
         update_node<Q, ST, ARITH>(f, rho, D.cp);
         store_node<Q, ST, true, MOVING>(dst, g, np, types, L, nb, node, rho, f);
@@ -785,8 +770,12 @@ template <int Q, int ST, bool MASK, int ARITH>
 int launch_fused(const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
                  const uint8_t* types, cudaStream_t st) {
     using T = typename Store<ST>::T;
-    nat_fused_k<Q, ST, MASK, ARITH><<<row_grid<Q>(g, 32), dim3(32, kRows), 0, st>>>(g, cp, np, (const T*)src,
-                                                                                    (T*)dst, types);
+    if (block_x(g, 1) == kBlockX)
+        nat_fused_k<Q, ST, MASK, ARITH, kBlockX><<<seg_grid(g, kBlockX, 1), kBlockX, 0, st>>>(
+            g, cp, np, (const T*)src, (T*)dst, types);
+    else
+        nat_fused_k<Q, ST, MASK, ARITH, 32><<<seg_grid(g, 32, 1), 32, 0, st>>>(g, cp, np, (const T*)src, (T*)dst,
+                                                                             types);
     return (int)cudaGetLastError();
 }
 
@@ -794,7 +783,7 @@ template <int Q, int ST, bool MASK, int ARITH>
 int launch_raw(const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
                const float* rho, const float* u, const uint8_t* types, cudaStream_t st) {
     using T = typename Store<ST>::T;
-    nat_collide_raw_k<Q, ST, MASK, ARITH><<<row_grid<Q>(g, 32), dim3(32, kRows), 0, st>>>(
+    nat_collide_raw_k<Q, ST, MASK, ARITH><<<cell_grid(g), kBlockX, 0, st>>>(
         g, cp, np, (const T*)src, (T*)dst, rho, u, types);
     return (int)cudaGetLastError();
 }
@@ -803,8 +792,7 @@ template <int Q, int ST, bool MASK>
 int launch_gather(const Geo& g, const NativeParams& np, const void* src, void* n_out, float* rho, float* u,
                   const uint8_t* types, cudaStream_t st) {
     using T = typename Store<ST>::T;
-    nat_gather_k<Q, ST, MASK><<<row_grid<Q>(g, 32), dim3(32, kRows), 0, st>>>(g, np, (const T*)src, (T*)n_out, rho,
-                                                                              u, types);
+    nat_gather_k<Q, ST, MASK><<<cell_grid(g), kBlockX, 0, st>>>(g, np, (const T*)src, (T*)n_out, rho, u, types);
     return (int)cudaGetLastError();
 }
 
@@ -833,14 +821,18 @@ auto with_storage_arith(int storage, int arith, F&& f) {
 template <int Q, int ARITH, bool MASK>
 int launch_fused_h2(const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
                     const uint8_t* types, cudaStream_t st) {
-    const dim3 grid = row_grid<Q>(g, 64);
-    const dim3 block(32, kRows);
-    if (MASK && np.moving)
-        nat_fused_h2_k<Q, true, true, ARITH><<<grid, block, 0, st>>>(g, cp, np, (const __half*)src, (__half*)dst,
-                                                                        types);
-    else
-        nat_fused_h2_k<Q, MASK, false, ARITH><<<grid, block, 0, st>>>(g, cp, np, (const __half*)src, (__half*)dst,
-                                                                         types);
+    auto go = [&](auto bxc) {
+        constexpr int BX = decltype(bxc)::value;
+        const dim3 grid = seg_grid(g, BX, 2);
+        if (MASK && np.moving)
+            nat_fused_h2_k<Q, true, true, ARITH, BX><<<grid, BX, 0, st>>>(g, cp, np, (const __half*)src,
+                                                                            (__half*)dst, types);
+        else
+            nat_fused_h2_k<Q, MASK, false, ARITH, BX><<<grid, BX, 0, st>>>(g, cp, np, (const __half*)src,
+                                                                             (__half*)dst, types);
+    };
+    if (block_x(g, 2) == kBlockX) go(std::integral_constant<int, kBlockX>{});
+    else go(std::integral_constant<int, 32>{});
     return (int)cudaGetLastError();
 }
 
@@ -875,19 +867,23 @@ template <int Q, int ST, bool MASK, int AR>
 int launch_aa(int kind, const Geo& g, const CollideParams& cp, const NativeParams& np, void* A, const float* rho,
               const float* u, const uint8_t* types, cudaStream_t st) {
     using T = typename Store<ST>::T;
-    const dim3 grid = row_grid<Q>(g, 32), block(32, kRows);
     const bool mv = MASK && np.moving;
-    auto go = [&](auto mvc) {
+    auto go = [&](auto mvc, auto bxc) {
         constexpr bool MV = decltype(mvc)::value;
+        constexpr int BX = decltype(bxc)::value;
+        const dim3 grid = seg_grid(g, BX, 1);
         if (kind == 0)
-            nat_aa_even_k<Q, ST, MASK, AR, MV, true><<<grid, block, 0, st>>>(g, cp, np, (T*)A, rho, u, types);
+            nat_aa_even_k<Q, ST, MASK, AR, MV, true, BX><<<grid, BX, 0, st>>>(g, cp, np, (T*)A, rho, u, types);
         else if (kind == 1)
-            nat_aa_even_k<Q, ST, MASK, AR, MV, false><<<grid, block, 0, st>>>(g, cp, np, (T*)A, rho, u, types);
+            nat_aa_even_k<Q, ST, MASK, AR, MV, false, BX><<<grid, BX, 0, st>>>(g, cp, np, (T*)A, rho, u, types);
         else
-            nat_aa_odd_k<Q, ST, MASK, AR, MV><<<grid, block, 0, st>>>(g, cp, np, (T*)A, types);
+            nat_aa_odd_k<Q, ST, MASK, AR, MV, BX><<<grid, BX, 0, st>>>(g, cp, np, (T*)A, types);
         return (int)cudaGetLastError();
     };
-    return mv ? go(std::true_type{}) : go(std::false_type{});
+    using W = std::integral_constant<int, kBlockX>;
+    using N = std::integral_constant<int, 32>;
+    if (block_x(g, 1) == kBlockX) return mv ? go(std::true_type{}, W{}) : go(std::false_type{}, W{});
+    return mv ? go(std::true_type{}, N{}) : go(std::false_type{}, N{});
 }
 
 template <bool TRT, int Q>
