@@ -315,6 +315,20 @@ int validate(const plb_params* p) {
     return PLB_OK;
 }
 
+// Page-locked host memory that the device can address (plb_host_alloc,
+// cudaHostAlloc, registered memory) is read or written by the layout kernels
+// directly over the host link: one pass instead of a copy plus a pass.
+// Returns null for other memory, which goes through the staging buffer.
+float* device_view(const void* host) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    return static_cast<float*>(a.devicePointer);
+}
+
 // Transfer buffer for one field of v components (grown on demand).
 int ensure_staging(plb_solve* s, int v) {
     const size_t cells = (size_t)(s->p.nx + 2) * (s->p.ny + 2) * (s->p.nz + 2);
@@ -827,18 +841,20 @@ int plb_get_field(plb_solve* s, int32_t which, float* out) {
     } else if (which == PLB_FIELD_RHO || which == PLB_FIELD_U) {
         PLB_TRY(ref_materialize_fields(s));
     }
-    PLB_TRY(ensure_staging(s, (int)(len / ((size_t)(s->p.nx + 2) * (s->p.ny + 2) * (s->p.nz + 2)))));
+    float* direct = device_view(out);
+    if (!direct) PLB_TRY(ensure_staging(s, (int)(len / ((size_t)(s->p.nx + 2) * (s->p.ny + 2) * (s->p.nz + 2)))));
+    float* aos = direct ? direct : s->staging;
     const float* wk = s->consts + s->q;
     if (which == PLB_FIELD_N || which == PLB_FIELD_NTMP) {
         const void* src = tmp ? tmp : s->f[which == PLB_FIELD_N ? n_buf : 1 - s->cur];
-        const int e = util_export(s->storage, s->q, s->g, src, wk, s->staging, s->stream);
+        const int e = util_export(s->storage, s->q, s->g, src, wk, aos, s->stream);
         if (tmp) cudaFreeAsync(tmp, s->stream);
         if (e != 0) return fail(PLB_ECUDA, std::string("util_export: ") + cudaGetErrorString((cudaError_t)e));
     } else {
         PLB_KERNEL(util_export(0, which == PLB_FIELD_RHO ? 1 : 3, s->g, which == PLB_FIELD_RHO ? s->rho : s->u,
-                               nullptr, s->staging, s->stream));
+                               nullptr, aos, s->stream));
     }
-    PLB_CUDA(cudaMemcpyAsync(out, s->staging, len * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    if (!direct) PLB_CUDA(cudaMemcpyAsync(out, s->staging, len * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
     return sync(s);
 }
 
@@ -853,13 +869,17 @@ int plb_set_field(plb_solve* s, int32_t which, const float* in) {
         PLB_TRY(ref_materialize_fields(s));
     }
     const size_t len = plb_field_len(s, which);
-    PLB_TRY(ensure_staging(s, (int)(len / ((size_t)(s->p.nx + 2) * (s->p.ny + 2) * (s->p.nz + 2)))));
-    PLB_CUDA(cudaMemcpyAsync(s->staging, in, len * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    const float* aos = device_view(in);
+    if (!aos) {
+        PLB_TRY(ensure_staging(s, (int)(len / ((size_t)(s->p.nx + 2) * (s->p.ny + 2) * (s->p.nz + 2)))));
+        PLB_CUDA(cudaMemcpyAsync(s->staging, in, len * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        aos = s->staging;
+    }
     if (which == PLB_FIELD_N || which == PLB_FIELD_NTMP) {
         void* dst = s->f[which == PLB_FIELD_N ? s->cur : 1 - s->cur];
-        PLB_KERNEL(util_import(s->storage, s->q, s->g, s->staging, s->consts + s->q, dst, s->stream));
+        PLB_KERNEL(util_import(s->storage, s->q, s->g, aos, s->consts + s->q, dst, s->stream));
     } else {
-        PLB_KERNEL(util_import(0, which == PLB_FIELD_RHO ? 1 : 3, s->g, s->staging, nullptr,
+        PLB_KERNEL(util_import(0, which == PLB_FIELD_RHO ? 1 : 3, s->g, aos, nullptr,
                                which == PLB_FIELD_RHO ? (void*)s->rho : (void*)s->u, s->stream));
         if (!s->native) s->fields_valid = true;
     }
@@ -927,6 +947,7 @@ struct plb_batch {
     int blocks = 0;
     int64_t cells = 0;
     bool moving = false;   // some member has a moving wall
+    bool pairs = false;    // FP16 with every nx even: the pair kernel, 64-node tasks
     int graph_steps = 64;
     cudaGraphExec_t graph = nullptr;
     std::vector<BatchDomain> h_doms;
@@ -992,7 +1013,7 @@ int batch_capture(plb_batch* b) {
     PLB_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     int rc = 0;
     for (int i = 0; i < b->graph_steps && rc == 0; ++i)
-        rc = nat_batch_step(b->q, b->storage, b->arith, b->moving, b->d_doms, b->d_tiles, b->ntiles, i & 1,
+        rc = nat_batch_step(b->q, b->storage, b->arith, b->moving, b->pairs, b->d_doms, b->d_tiles, b->ntiles, i & 1,
                             b->blocks, b->stream);
     const cudaError_t ec = cudaStreamEndCapture(b->stream, &graph);
     if (rc != 0) {
@@ -1036,19 +1057,22 @@ int plb_batch_create(int32_t n, plb_solve* const* solves, plb_batch** out) {
         batch_release(b);
         return fail(PLB_ECUDA, "cudaStreamCreate");
     }
+    b->pairs = b->storage == PLB_STORAGE_FP16_DEV;
+    for (int i = 0; i < n; ++i) b->pairs = b->pairs && solves[i]->g.nx % 2 == 0;
+    const int per_task = b->pairs ? 64 : 32;
     std::vector<int4> tiles;
     for (int i = 0; i < n; ++i) {
         const Geo& g = solves[i]->g;
         const int plane = g.nx * g.ny;   // nodes of one z plane, x fastest
         for (int z = 0; z < g.nz; ++z)
-            for (int i0 = 0; i0 < plane; i0 += 32) tiles.push_back(make_int4(i, z, i0, 0));
+            for (int i0 = 0; i0 < plane; i0 += per_task) tiles.push_back(make_int4(i, z, i0, 0));
         b->cells += g.cells();
     }
     b->ntiles = (int)tiles.size();
     int dev_sms = 0;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, b->device);
     for (int i = 0; i < n; ++i) b->moving |= solves[i]->np.moving != 0;
-    const int per_sm = nat_batch_blocks_per_sm(b->q, b->storage, b->arith, b->moving);
+    const int per_sm = nat_batch_blocks_per_sm(b->q, b->storage, b->arith, b->moving, b->pairs);
     b->blocks = (dev_sms > 0 ? dev_sms : 1) * (per_sm > 0 ? per_sm : 1);
     // stream-ordered, like a solve's memory
     if (cudaMallocAsync(&b->d_doms, n * sizeof(BatchDomain), b->stream) != cudaSuccess ||
@@ -1084,7 +1108,7 @@ int plb_batch_step_async(plb_batch* b, int64_t nsteps) {
         i += G;
     }
     for (; i < todo; ++i)
-        PLB_KERNEL(nat_batch_step(b->q, b->storage, b->arith, b->moving, b->d_doms, b->d_tiles, b->ntiles, (int)(i & 1),
+        PLB_KERNEL(nat_batch_step(b->q, b->storage, b->arith, b->moving, b->pairs, b->d_doms, b->d_tiles, b->ntiles, (int)(i & 1),
                                   b->blocks, b->stream));
     if (todo & 1)
         for (plb_solve* s : b->solves) s->cur = 1 - s->cur;

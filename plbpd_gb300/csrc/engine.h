@@ -107,10 +107,12 @@ struct BatchDomain {
 // One launch advances every domain by one step, reading f[parity] and
 // writing f[parity ^ 1]; `blocks` resident blocks walk the task list.
 // `moving`: some member has a moving wall.
-int nat_batch_step(int q, int storage, int arith, bool moving, const BatchDomain* doms, const int4* tiles,
-                   int ntiles, int parity, int blocks, cudaStream_t st);
+// `pairs`: FP16 storage, every domain's nx even, tasks of 64 nodes: the pair
+// kernel's work.
+int nat_batch_step(int q, int storage, int arith, bool moving, bool pairs, const BatchDomain* doms,
+                   const int4* tiles, int ntiles, int parity, int blocks, cudaStream_t st);
 // Resident blocks per SM of the batch kernel (for sizing the grid).
-int nat_batch_blocks_per_sm(int q, int storage, int arith, bool moving);
+int nat_batch_blocks_per_sm(int q, int storage, int arith, bool moving, bool pairs);
 constexpr int kBatchTile = 128;
 
 // The TRT instantiations behind the functions above (kernels_trt.cu).
@@ -122,9 +124,9 @@ int nat_collide_raw_trt(int q, int storage, bool has_mask, const Geo& g, const C
 int nat_aa_step_trt(int kind, int q, int storage, bool has_mask, const Geo& g, const CollideParams& cp,
                     const NativeParams& np, void* A, const float* rho, const float* u, const uint8_t* types,
                     cudaStream_t st);
-int nat_batch_blocks_per_sm_trt(int q, int storage, bool moving);
-int nat_batch_step_trt(int q, int storage, bool moving, const BatchDomain* doms, const int4* tiles, int ntiles,
-                       int parity, int blocks, cudaStream_t st);
+int nat_batch_blocks_per_sm_trt(int q, int storage, bool moving, bool pairs);
+int nat_batch_step_trt(int q, int storage, bool moving, bool pairs, const BatchDomain* doms, const int4* tiles,
+                       int ntiles, int parity, int blocks, cudaStream_t st);
 
 // ---- shared (kernels_util.cu) ----------------------------------------------
 // Every node of the box (halo included): rho0, u0, n = feq, ntmp = 0.

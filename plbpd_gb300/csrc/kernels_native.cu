@@ -19,6 +19,7 @@
 //   1  FP16 deviations d_k = f_k - w_k, arithmetic in FP32 in deviation form
 //   2  FP64 populations and FP64 arithmetic: the reference run of the same
 //      method that reduced-precision runs are measured against
+//   3  FP32 deviations d_k = f_k - w_k with storage 1's arithmetic
 #include "native_impl.cuh"
 
 namespace plb {
@@ -170,15 +171,16 @@ int nat_aa_gather(int q, int storage, bool has_mask, bool swapped, const Geo& g,
 #undef CALL
 }
 
-int nat_batch_blocks_per_sm(int q, int storage, int arith, bool moving) {
-    if (arith == kArithTRT) return nat_batch_blocks_per_sm_trt(q, storage, moving);
-    return batch_blocks_per_sm<false>(q, storage, arith, moving);
+int nat_batch_blocks_per_sm(int q, int storage, int arith, bool moving, bool pairs) {
+    if (arith == kArithTRT) return nat_batch_blocks_per_sm_trt(q, storage, moving, pairs);
+    return batch_blocks_per_sm<false>(q, storage, arith, moving, pairs);
 }
 
-int nat_batch_step(int q, int storage, int arith, bool moving, const BatchDomain* doms, const int4* tiles,
-                   int ntiles, int parity, int blocks, cudaStream_t st) {
-    if (arith == kArithTRT) return nat_batch_step_trt(q, storage, moving, doms, tiles, ntiles, parity, blocks, st);
-    return batch_step<false>(q, storage, arith, moving, doms, tiles, ntiles, parity, blocks, st);
+int nat_batch_step(int q, int storage, int arith, bool moving, bool pairs, const BatchDomain* doms,
+                   const int4* tiles, int ntiles, int parity, int blocks, cudaStream_t st) {
+    if (arith == kArithTRT)
+        return nat_batch_step_trt(q, storage, moving, pairs, doms, tiles, ntiles, parity, blocks, st);
+    return batch_step<false>(q, storage, arith, moving, pairs, doms, tiles, ntiles, parity, blocks, st);
 }
 
 int nat_reset_fields(const Geo& g, const NativeParams& np, const uint8_t* types, float* rho, float* u,

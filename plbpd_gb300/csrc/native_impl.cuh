@@ -413,15 +413,16 @@ nat_fused_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::
 // and measured 1.6x (D3Q19) to 2.3x (D3Q27) slower.  A source row outside a
 // walled axis only occurs for pairs in a wall row, which are solid and store
 // nothing; its address is clamped to the pair's own row.
-template <int Q, bool MASK, bool MOVING, int ARITH, int BX>
-__global__ void __launch_bounds__(BX)
-nat_fused_h2_k(Geo g, CollideParams cp, NativeParams np, const __half* __restrict__ src, __half* __restrict__ dst,
-               const uint8_t* __restrict__ types) {
+// One lane's pair (x0, x0 + 1) of row (y, z); every lane of the warp calls
+// it together (the shuffles), lanes past the end of their row with
+// active = false.  A lane's neighbour lane holds the neighbouring pair of the
+// same row unless x0 is 0 or x0 + 2 is nx, which the edge loads cover.
+template <int Q, bool MASK, bool MOVING, int ARITH>
+__device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, const NativeParams& np,
+                                        const __half* __restrict__ src, __half* __restrict__ dst,
+                                        const uint8_t* __restrict__ types, int lane, int x0, int y, int z,
+                                        bool active) {
     const unsigned kFull = 0xffffffffu;
-    const int lane = threadIdx.x & 31;   // a warp is 32 consecutive pairs of one row
-    const int x0 = 2 * (blockIdx.x * BX + threadIdx.x);
-    const int y = blockIdx.y, z = blockIdx.z;
-    const bool active = x0 < g.nx;
     const int ym = y == 0 ? (g.wrap_y ? g.ny - 1 : y) : y - 1;
     const int yp = y == g.ny - 1 ? (g.wrap_y ? 0 : y) : y + 1;
     const int zm = z == 0 ? (g.wrap_z ? g.nz - 1 : z) : z - 1;
@@ -502,6 +503,15 @@ nat_fused_h2_k(Geo g, CollideParams cp, NativeParams np, const __half* __restric
         __stcs(reinterpret_cast<unsigned int*>(dst + (long long)k * g.ks + node0),
                *reinterpret_cast<const unsigned int*>(&v));
     }
+}
+
+template <int Q, bool MASK, bool MOVING, int ARITH, int BX>
+__global__ void __launch_bounds__(BX)
+nat_fused_h2_k(Geo g, CollideParams cp, NativeParams np, const __half* __restrict__ src, __half* __restrict__ dst,
+               const uint8_t* __restrict__ types) {
+    const int lane = threadIdx.x & 31;   // a warp is 32 consecutive pairs of one row
+    const int x0 = 2 * (blockIdx.x * BX + threadIdx.x);
+    h2_pair<Q, MASK, MOVING, ARITH>(g, cp, np, src, dst, types, lane, x0, blockIdx.y, blockIdx.z, x0 < g.nx);
 }
 
 // First collision from a RAW state: n at the node itself and the rho/u fields.
@@ -764,6 +774,28 @@ nat_batch_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks
     }
 }
 
+// FP16 batches of domains with even nx: the pair kernel's work over warp
+// tasks of 64 consecutive nodes (32 pairs) of one z plane.  A pair never
+// straddles a row (nx is even), and the rows of a warp's pairs differ, so
+// each lane forms its own row offsets.
+template <int Q, int ARITH, bool MOVING>
+__global__ void __launch_bounds__(kBatchTile)
+nat_batch_h2_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks, int ntasks, int parity) {
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (kBatchTile / 32);
+    for (int t = blockIdx.x * (kBatchTile / 32) + (threadIdx.x >> 5); t < ntasks; t += warps) {
+        const int4 tk = __ldg(tasks + t);
+        const BatchDomain& D = doms[tk.x];
+        const Geo g = D.g;
+        const int i = tk.z + 2 * lane;
+        const bool active = i < g.nx * g.ny;
+        const int y = active ? (int)((unsigned)i / (unsigned)g.nx) : 0;
+        const int x0 = active ? i - y * g.nx : 0;
+        h2_pair<Q, true, MOVING, ARITH>(g, D.cp, D.np, static_cast<const __half*>(D.f[parity]),
+                                        static_cast<__half*>(D.f[parity ^ 1]), D.types, lane, x0, y, tk.y, active);
+    }
+}
+
 dim3 cell_grid(const Geo& g) { return dim3((g.nx + kBlockX - 1) / kBlockX, g.ny, g.nz); }
 
 template <int Q, int ST, bool MASK, int ARITH>
@@ -896,13 +928,22 @@ int aa_q(int kind, int storage, int arith, bool m, const Geo& g, const CollidePa
     });
 }
 
-// Batches hold FP32 or FP16 storage.
+// Batches hold FP32, FP32-deviation or FP16 storage; `pairs`: FP16 batches
+// whose domains all have even nx run the pair kernel over 64-node tasks.
 template <bool TRT, bool MV>
-const void* batch_kernel_for(int q, int storage, int arith) {
+const void* batch_kernel_for(int q, int storage, int arith, bool pairs) {
     if (storage == 2) return nullptr;
     const void* k = nullptr;
     with_storage_arith<TRT>(storage, arith, [&](auto stc, auto arc) {
         constexpr int ST = decltype(stc)::value == 2 ? 0 : decltype(stc)::value, AR = decltype(arc)::value;
+        if constexpr (ST == 1) {
+            if (pairs) {
+                k = q == 9 ? (const void*)nat_batch_h2_k<9, AR, MV>
+                  : q == 19 ? (const void*)nat_batch_h2_k<19, AR, MV>
+                  : q == 27 ? (const void*)nat_batch_h2_k<27, AR, MV> : nullptr;
+                return 0;
+            }
+        }
         k = q == 9 ? (const void*)nat_batch_k<9, ST, AR, MV>
           : q == 19 ? (const void*)nat_batch_k<19, ST, AR, MV>
           : q == 27 ? (const void*)nat_batch_k<27, ST, AR, MV> : nullptr;
@@ -912,9 +953,9 @@ const void* batch_kernel_for(int q, int storage, int arith) {
 }
 
 template <bool TRT>
-int batch_blocks_per_sm(int q, int storage, int arith, bool moving) {
-    const void* k = moving ? batch_kernel_for<TRT, true>(q, storage, arith)
-                           : batch_kernel_for<TRT, false>(q, storage, arith);
+int batch_blocks_per_sm(int q, int storage, int arith, bool moving, bool pairs) {
+    const void* k = moving ? batch_kernel_for<TRT, true>(q, storage, arith, pairs)
+                           : batch_kernel_for<TRT, false>(q, storage, arith, pairs);
     if (!k) return 0;
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kBatchTile, 0) != cudaSuccess) return 0;
@@ -922,8 +963,8 @@ int batch_blocks_per_sm(int q, int storage, int arith, bool moving) {
 }
 
 template <bool TRT>
-int batch_step(int q, int storage, int arith, bool moving, const BatchDomain* doms, const int4* tiles, int ntiles,
-               int parity, int blocks, cudaStream_t st) {
+int batch_step(int q, int storage, int arith, bool moving, bool pairs, const BatchDomain* doms, const int4* tiles,
+               int ntiles, int parity, int blocks, cudaStream_t st) {
     if (ntiles <= 0) return 0;
     if (storage == 2) return (int)cudaErrorInvalidValue;
     const int need = (ntiles + kBatchTile / 32 - 1) / (kBatchTile / 32);   // one task per warp
@@ -932,6 +973,15 @@ int batch_step(int q, int storage, int arith, bool moving, const BatchDomain* do
         constexpr int ST = decltype(stc)::value == 2 ? 0 : decltype(stc)::value, AR = decltype(arc)::value;
         auto go = [&](auto qc) {
             constexpr int Q = decltype(qc)::value;
+            if constexpr (ST == 1) {
+                if (pairs) {
+                    if (moving)
+                        nat_batch_h2_k<Q, AR, true><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);
+                    else
+                        nat_batch_h2_k<Q, AR, false><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);
+                    return (int)cudaGetLastError();
+                }
+            }
             if (moving) nat_batch_k<Q, ST, AR, true><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);
             else nat_batch_k<Q, ST, AR, false><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);
             return (int)cudaGetLastError();

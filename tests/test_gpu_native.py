@@ -173,3 +173,35 @@ def test_fp32_deviation_storage_accuracy():
             err[name] = rel_l2(s.get(3)[1:-1, 1:-1, 1:-1], u64)
     assert err["fp32dev"] < 1e-4, err
     assert err["fp32dev"] < err["fp32"] / 10, err
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_pinned_host_buffers_transfer_directly(storage):
+    """Page-locked host buffers are read and written by the layout kernels
+    directly; the bytes equal the staged path's for every field."""
+    from plbpd_gb300 import capi
+    cfg = NATIVE_CASES["obstacles_d3q19"]
+    mask = mask_for("obstacles_d3q19", cfg)
+    st = capi.STORAGE_FP16_DEV if storage == "fp16" else capi.STORAGE_FP32
+    with capi.Solve.create(**cfg, semantics=capi.SEMANTICS_NATIVE, arith=capi.ARITH_FP32, storage=st) as s:
+        s.set_mask(mask)
+        s.initialize()
+        s.step(5)
+        for w in (capi.FIELD_N, capi.FIELD_RHO, capi.FIELD_U):
+            pinned = capi.PinnedBuffer(s.shape(w))
+            s.get(w, pinned.array)
+            assert_bitexact(pinned.array, s.get(w), f"get {w}")
+            pinned.free()
+        n = s.get(capi.FIELD_N)
+        n[1:-1, 1:-1, 1:-1] *= np.float32(1.0001)
+        pn = capi.PinnedBuffer(s.shape(capi.FIELD_N))
+        pn.array[...] = n
+        s.set(capi.FIELD_N, pn.array)
+        got = s.get(capi.FIELD_N)
+        with capi.Solve.create(**cfg, semantics=capi.SEMANTICS_NATIVE, arith=capi.ARITH_FP32, storage=st) as t:
+            t.set_mask(mask)
+            t.initialize()
+            t.step(5)
+            t.set(capi.FIELD_N, n)
+            assert_bitexact(got, t.get(capi.FIELD_N), "set n")
+        pn.free()
