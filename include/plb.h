@@ -246,6 +246,7 @@ typedef struct plb_request {
 #define PLB_REQ_RUNNING 1
 #define PLB_REQ_DONE 2
 #define PLB_REQ_FAILED 3
+#define PLB_REQ_CANCELLED 4
 /* Device bytes a solve with these parameters holds while it runs. */
 int64_t plb_solve_bytes(const plb_params* params);
 /* tick_steps: most steps a class advances between admission checks. */
@@ -253,6 +254,11 @@ int plb_server_start(int32_t device, int64_t budget_bytes, int32_t tick_steps, p
 /* Thread-safe; the request (and its mask) is copied.  *id names it later. */
 int plb_server_submit(plb_server* srv, const plb_request* req, int64_t* id);
 int plb_server_status(plb_server* srv, int64_t id, int32_t* state);
+/* Cancels a request: a queued one never starts; a running one stops when its
+ * current tick ends and its memory returns to the budget.  Either then
+ * reports PLB_REQ_CANCELLED, and wait/result return PLB_ESTATE for it.
+ * PLB_ESTATE for a request that already finished. */
+int plb_server_cancel(plb_server* srv, int64_t id);
 /* Blocks until the request is done or failed, or timeout_s passes (PLB_ETIMEOUT). */
 int plb_server_wait(plb_server* srv, int64_t id, double timeout_s);
 /* Copies a finished request's rho (plb_field_len RHO floats) and u (U floats)

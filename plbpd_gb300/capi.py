@@ -23,7 +23,7 @@ COLLISION_BGK, COLLISION_TRT = 0, 1
 STREAMING_AB, STREAMING_AA = 0, 1
 STORAGE_FP32, STORAGE_FP16_DEV, STORAGE_FP64, STORAGE_FP32_DEV = 0, 1, 2, 3
 FIELD_N, FIELD_NTMP, FIELD_RHO, FIELD_U = 0, 1, 2, 3
-REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = 0, 1, 2, 3, 4
 Q_OF = {"D2Q9": 9, "D3Q19": 19, "D3Q27": 27}
 
 
@@ -85,6 +85,7 @@ _SIGS = [
     ("plb_server_start", C.c_int, [C.c_int32, C.c_int64, C.c_int32, C.POINTER(C.c_void_p)]),
     ("plb_server_submit", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]),
     ("plb_server_status", C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int32)]),
+    ("plb_server_cancel", C.c_int, [C.c_void_p, C.c_int64]),
     ("plb_server_wait", C.c_int, [C.c_void_p, C.c_int64, C.c_double]),
     ("plb_server_result", C.c_int, [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("plb_server_memory", C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
@@ -346,6 +347,9 @@ class Server:
         st = C.c_int32()
         check(lib().plb_server_status(self.h, int(rid), C.byref(st)))
         return st.value
+
+    def cancel(self, rid: int) -> None:
+        check(lib().plb_server_cancel(self.h, int(rid)))
 
     def wait(self, rid: int, timeout_s: float = 600.0) -> None:
         check(lib().plb_server_wait(self.h, int(rid), float(timeout_s)))

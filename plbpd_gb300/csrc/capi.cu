@@ -1,6 +1,7 @@
 // The C ABI (include/plb.h): handle lifetime, validation, state tracking,
 // step orchestration (CUDA-graph chunks of fused steps) and transfers between
 // host buffers in plbpd's layout and the device layout.
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -269,6 +270,16 @@ int validate(const plb_params* p) {
     if (p->q != 9 && p->q != 19 && p->q != 27)
         return fail(PLB_EINVAL, "Model with " + std::to_string(p->q) + " directions not yet implemented");
     if (p->nx < 1 || p->ny < 1 || p->nz < 1) return fail(PLB_EINVAL, "argument is zero");
+    {
+        // a request with a NaN or infinite parameter fails here, not in the kernels
+        bool finite = std::isfinite(p->nu) && std::isfinite(p->rho0) && std::isfinite(p->rho_solid) &&
+                      std::isfinite(p->trt_magic);
+        for (int i = 0; i < 3; ++i) finite = finite && std::isfinite(p->u0[i]) && std::isfinite(p->force[i]);
+        for (int f = 0; f < 6; ++f)
+            for (int i = 0; i < 3; ++i) finite = finite && std::isfinite(p->face_vel[f][i]);
+        if (!finite) return fail(PLB_EINVAL, "parameters must be finite");
+        if (!(3.0f * p->nu + 0.5f > 0.0f)) return fail(PLB_EINVAL, "tau = 3 nu + 1/2 must be positive");
+    }
     if (p->ny > 65535 || p->nz > 65535 || p->nx > (1ll << 30))
         return fail(PLB_EINVAL, "domain extent too large (ny, nz <= 65535)");
     for (int f = 0; f < 6; ++f) {
@@ -506,6 +517,8 @@ int sync(plb_solve* s) {
 }
 
 }  // namespace
+
+int plb::check_params(const plb_params* p) { return validate(p); }
 
 // ===========================================================================
 extern "C" {

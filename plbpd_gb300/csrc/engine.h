@@ -7,10 +7,16 @@
 
 #include "lattice.cuh"
 
+struct plb_params;
+
 namespace plb {
 
 // Stores the message plb_last_error() returns on this thread.
 void record_error(const std::string& msg);
+
+// plb_solve_create's checks of a parameter block: PLB_OK, or an error code
+// with the message recorded.
+int check_params(const plb_params* p);
 
 // Boundary description handed to the REFERENCE-semantics kernels.  Faces are
 // numbered east, west, north, south, up, down (plbpd's src/Boundary.cpp:17-18).

@@ -18,6 +18,7 @@
 // so one lane's tick never waits for another's.  Device memory is
 // stream-ordered, so retiring a solve does not synchronize the device.
 // Clients submit from any thread and wait on a condition variable.
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstdlib>
@@ -38,6 +39,7 @@
 
 namespace plb {
 void record_error(const std::string& msg);   // capi.cu: the plb_last_error() slot
+int check_params(const plb_params* p);       // capi.cu: plb_solve_create's validation
 }
 
 namespace {
@@ -55,6 +57,7 @@ struct Req {
     plb_solve* s = nullptr;
     std::vector<float> rho, u;
     std::string err;
+    std::atomic<bool> cancel{false};   // set by plb_server_cancel while it runs
 };
 
 // A unit of running work with its own stream: one batch of small solves of a
@@ -148,6 +151,14 @@ void retire(plb_server* srv, Req* r) {
     finish(srv, r, err.empty() ? PLB_REQ_DONE : PLB_REQ_FAILED, err);
 }
 
+// A running request cancelled by its client: its solve is destroyed and
+// its bytes return to the budget; there is no result.
+void drop_cancelled(plb_server* srv, Req* r) {
+    if (r->s) plb_solve_destroy(r->s);
+    r->s = nullptr;
+    finish(srv, r, PLB_REQ_CANCELLED, "request was cancelled");
+}
+
 void fail_lane(plb_server* srv, Lane& L, const std::string& e) {
     if (L.batch) plb_batch_destroy(L.batch);
     L.batch = nullptr;
@@ -204,7 +215,10 @@ bool collect_tick(plb_server* srv, Lane& L) {
     std::vector<Req*> keep;
     for (Req* r : L.members) {
         r->remaining -= L.inflight;
-        if (r->remaining <= 0) {
+        if (r->cancel) {
+            drop_cancelled(srv, r);
+            L.dirty = true;
+        } else if (r->remaining <= 0) {
             retire(srv, r);
             L.dirty = true;
         } else {
@@ -275,7 +289,10 @@ void scheduler(plb_server* srv) {
         auto service = [&](Lane& L) {
             if (L.inflight && !collect_tick(srv, L)) return;
             if (!L.joining.empty()) {
-                L.members.insert(L.members.end(), L.joining.begin(), L.joining.end());
+                for (Req* r : L.joining) {
+                    if (r->cancel) drop_cancelled(srv, r);
+                    else L.members.push_back(r);
+                }
                 L.joining.clear();
                 L.dirty = true;
             }
@@ -364,6 +381,10 @@ int plb_server_submit(plb_server* srv, const plb_request* req, int64_t* id) {
         plb::record_error("served requests need NATIVE semantics and at least one step");
         return PLB_EINVAL;
     }
+    // malformed requests (a NaN viscosity, an unknown lattice, ...) are refused
+    // here, on the caller's thread, with plb_solve_create's message
+    const int v = plb::check_params(&req->params);
+    if (v != PLB_OK) return v;
     auto r = std::make_unique<Req>();
     r->p = req->params;
     r->steps = r->remaining = req->steps;
@@ -394,12 +415,16 @@ int plb_server_wait(plb_server* srv, int64_t id, double timeout_s) {
     if (it == srv->reqs.end()) return PLB_EINVAL;
     Req* r = it->second.get();
     const bool ok = srv->done_cv.wait_for(lk, std::chrono::duration<double>(timeout_s), [&] {
-        return r->state == PLB_REQ_DONE || r->state == PLB_REQ_FAILED;
+        return r->state == PLB_REQ_DONE || r->state == PLB_REQ_FAILED || r->state == PLB_REQ_CANCELLED;
     });
     if (!ok) return PLB_ETIMEOUT;
     if (r->state == PLB_REQ_FAILED) {
         plb::record_error(r->err);
         return PLB_ECUDA;
+    }
+    if (r->state == PLB_REQ_CANCELLED) {
+        plb::record_error(r->err);
+        return PLB_ESTATE;
     }
     return PLB_OK;
 }
@@ -411,10 +436,11 @@ int plb_server_result(plb_server* srv, int64_t id, float* rho, float* u, double*
         std::lock_guard<std::mutex> lk(srv->mu);
         auto it = srv->reqs.find(id);
         if (it == srv->reqs.end()) return PLB_EINVAL;
-        if (it->second->state == PLB_REQ_FAILED) {
+        if (it->second->state == PLB_REQ_FAILED || it->second->state == PLB_REQ_CANCELLED) {
             plb::record_error(it->second->err);
+            const int rc = it->second->state == PLB_REQ_FAILED ? PLB_ECUDA : PLB_ESTATE;
             srv->reqs.erase(it);
-            return PLB_ECUDA;
+            return rc;
         }
         if (it->second->state != PLB_REQ_DONE) return PLB_ESTATE;
         r = std::move(it->second);
@@ -424,6 +450,32 @@ int plb_server_result(plb_server* srv, int64_t id, float* rho, float* u, double*
     if (u) std::memcpy(u, r->u.data(), r->u.size() * sizeof(float));
     if (times3) { times3[0] = r->t_sub; times3[1] = r->t_adm; times3[2] = r->t_done; }
     return PLB_OK;
+}
+
+int plb_server_cancel(plb_server* srv, int64_t id) {
+    if (!srv) return PLB_EINVAL;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    auto it = srv->reqs.find(id);
+    if (it == srv->reqs.end()) return PLB_EINVAL;
+    Req* r = it->second.get();
+    if (r->state == PLB_REQ_QUEUED) {
+        for (auto q = srv->pending.begin(); q != srv->pending.end(); ++q)
+            if (*q == r) {
+                srv->pending.erase(q);
+                break;
+            }
+        r->state = PLB_REQ_CANCELLED;
+        r->err = "request was cancelled";
+        r->t_done = srv->now();
+        srv->done_cv.notify_all();
+        return PLB_OK;
+    }
+    if (r->state == PLB_REQ_RUNNING) {
+        r->cancel = true;   // the scheduler drops it when its current tick ends
+        return PLB_OK;
+    }
+    plb::record_error("request already finished");
+    return PLB_ESTATE;
 }
 
 int plb_server_memory(plb_server* srv, int64_t* in_use, int64_t* peak) {

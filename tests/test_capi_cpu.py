@@ -88,7 +88,12 @@ def test_invalid_parameters_rejected_before_any_device_work(lib):
     bad = [dict(model="D3Q19", nx=0, ny=4, nz=4, nu=0.1),
            dict(model="D3Q19", nx=4, ny=4, nz=4, nu=0.1, semantics=capi.SEMANTICS_NATIVE,
                 face_type={"east": "periodic", "west": "noslip"}),
-           dict(model="D3Q19", nx=4, ny=4, nz=4, nu=0.1, storage=capi.STORAGE_FP16_DEV)]
+           dict(model="D3Q19", nx=4, ny=4, nz=4, nu=0.1, storage=capi.STORAGE_FP16_DEV),
+           # non-finite parameters and tau <= 0 never reach a kernel
+           dict(model="D3Q19", nx=4, ny=4, nz=4, nu=float("nan")),
+           dict(model="D3Q19", nx=4, ny=4, nz=4, nu=0.1, force=(float("inf"), 0.0, 0.0)),
+           dict(model="D2Q9", nx=4, ny=1, nz=4, nu=0.1, rho0=float("nan")),
+           dict(model="D3Q19", nx=4, ny=4, nz=4, nu=-0.2)]
     for kw in bad:
         with pytest.raises(capi.PlbError) as e:
             capi.Solve.create(**kw)

@@ -2,6 +2,7 @@
 step count run together (continuous batching) and each result equals the
 same request run alone; admission respects the memory budget."""
 import threading
+import time
 
 import numpy as np
 import pytest
@@ -107,3 +108,95 @@ def test_concurrent_submitters():
     for k, (p, m, n) in enumerate(reqs):
         _, u_a = run_alone(capi, p, m, n)
         assert np.array_equal(out[k].view(np.uint32), u_a.view(np.uint32))
+
+
+def test_malformed_request_refused_at_submit():
+    """A NaN viscosity is refused on the submitting thread; the requests
+    around it are unaffected."""
+    from plbpd_gb300 import capi
+    rng = np.random.default_rng(5)
+    good = [request_params(capi, rng, "D2Q9", capi.STORAGE_FP32) for _ in range(2)]
+    bad, bm, bn = request_params(capi, rng, "D2Q9", capi.STORAGE_FP32)
+    bad.nu = float("nan")
+    with capi.Server(budget_bytes=2 << 30, tick_steps=40) as srv:
+        r0 = srv.submit(good[0][0], good[0][2], good[0][1])
+        with pytest.raises(capi.PlbError) as e:
+            srv.submit(bad, bn, bm)
+        assert e.value.code == capi.EINVAL
+        r1 = srv.submit(good[1][0], good[1][2], good[1][1])
+        out = []
+        for rid in (r0, r1):
+            srv.wait(rid, 300.0)
+            out.append(srv.result(rid)[1])
+    for (p, m, n), u in zip(good, out):
+        assert np.array_equal(u.view(np.uint32), run_alone(capi, p, m, n)[1].view(np.uint32))
+
+
+def test_cancel_queued_and_running_requests():
+    """Cancelling a queued request drops it before admission; cancelling a
+    running one ends it at the next tick and returns its memory; a request
+    run beside them still equals its solo run."""
+    from plbpd_gb300 import capi
+    rng = np.random.default_rng(9)
+    big_p, big_m, _ = request_params(capi, rng, "D3Q19", capi.STORAGE_FP32)
+    small = request_params(capi, rng, "D2Q9", capi.STORAGE_FP32)
+    budget = int(capi.lib().plb_solve_bytes(capi.C.byref(big_p)) * 1.2)
+    with capi.Server(budget_bytes=budget, tick_steps=20) as srv:
+        running = srv.submit(big_p, 2_000_000, big_m)      # holds the budget
+        queued = srv.submit(big_p, 50, big_m)              # waits for it
+        for _ in range(2000):
+            if srv.status(running) == capi.REQ_RUNNING:
+                break
+            time.sleep(0.005)
+        assert srv.status(running) == capi.REQ_RUNNING
+        assert srv.status(queued) == capi.REQ_QUEUED
+        srv.cancel(queued)
+        assert srv.status(queued) == capi.REQ_CANCELLED
+        srv.cancel(running)
+        with pytest.raises(capi.PlbError) as e:
+            srv.wait(running, 120.0)
+        assert e.value.code == capi.ESTATE
+        assert srv.status(running) == capi.REQ_CANCELLED
+        with pytest.raises(capi.PlbError):
+            srv.result(running)
+        with pytest.raises(capi.PlbError):
+            srv.result(queued)
+        in_use, _ = srv.memory()
+        assert in_use == 0
+        p, m, n = small
+        rid = srv.submit(p, n, m)
+        srv.wait(rid, 300.0)
+        u = srv.result(rid)[1]
+    assert np.array_equal(u.view(np.uint32), run_alone(capi, p, m, n)[1].view(np.uint32))
+
+
+def test_failing_client_does_not_disturb_others():
+    """A client thread that raises after submitting (and never collects) leaves
+    the other clients' results exact."""
+    from plbpd_gb300 import capi
+    rng = np.random.default_rng(13)
+    reqs = [request_params(capi, rng, "D2Q9", capi.STORAGE_FP16_DEV) for _ in range(4)]
+    out, errors = {}, []
+    with capi.Server(budget_bytes=4 << 30, tick_steps=32) as srv:
+        def client(k):
+            p, m, n = reqs[k]
+            rid = srv.submit(p, n, m)
+            if k == 0:
+                raise RuntimeError("client gave up")
+            srv.wait(rid, 300.0)
+            out[k] = srv.result(rid)[1]
+
+        def guarded(k):
+            try:
+                client(k)
+            except RuntimeError as ex:
+                errors.append(str(ex))
+        th = [threading.Thread(target=guarded, args=(k,)) for k in range(len(reqs))]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+    assert errors == ["client gave up"]
+    for k in range(1, len(reqs)):
+        p, m, n = reqs[k]
+        assert np.array_equal(out[k].view(np.uint32), run_alone(capi, p, m, n)[1].view(np.uint32))
