@@ -131,6 +131,10 @@ struct CollideParams {
     // gp = 1 - omega/2, gm = 1 - omega_m/2 (float arithmetic)
     float omega_m, gp, gm;
     double omega_m_d;
+    // -0.0f, known only at run time: the addend that makes a fused
+    // multiply-add an exact product the paired-FP32 code can use where a
+    // product feeds a sum (native_impl.cuh, mulx2)
+    float neg_zero = -0.0f;
 };
 
 // Kernel arithmetic: plbpd's (FP32 body + FP64 tail), FP32 only, or the

@@ -288,6 +288,206 @@ __device__ __forceinline__ void update_node(typename Store<ST>::R (&f)[Q], typen
     }
 }
 
+// ---- two nodes per instruction: Blackwell's paired FP32 operations ----------
+// add/sub/mul/fma.rn.f32x2 apply one FP32 operation to both halves of a
+// float2, each half rounded exactly as the scalar operation.  The FP16 pair
+// kernel holds two x-neighbour nodes per thread; updating them through these
+// operations, op for op as the scalar update_node<Q, 1, ARITH>, gives the
+// same bits with half the FP32 math instructions (the divisions stay scalar:
+// there is no paired divide).
+//
+// ptxas merges a paired multiply into a paired add or subtract that consumes
+// it (a fused multiply-add, one rounding instead of two) even when the PTX
+// names the rounding mode and -fmad=false is given, and it also recognises a
+// multiply-add with a constant -0 addend as a multiply.  A product that feeds
+// a sum is therefore formed by mulx2: a multiply-add whose -0 addend comes
+// from the kernel parameters, which rounds exactly as the product (x*y + -0
+// is x*y, zeros keep their sign) and cannot be merged further.
+__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ unsigned long long f2bits(float2 a) {
+    return *reinterpret_cast<const unsigned long long*>(&a);
+}
+__device__ __forceinline__ float2 bits2f(unsigned long long d) { return *reinterpret_cast<const float2*>(&d); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2bits(a)), "l"(f2bits(b)));
+    return bits2f(d);
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2bits(a)), "l"(f2bits(b)));
+    return bits2f(d);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2bits(a)), "l"(f2bits(b)));
+    return bits2f(d);
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2bits(a)), "l"(f2bits(b)), "l"(f2bits(c)));
+    return bits2f(d);
+}
+__device__ __forceinline__ float2 mulx2(float2 a, float2 b, float2 nz) { return fma2(a, b, nz); }
+__device__ __forceinline__ float2 div2(float a, float2 b) { return make_float2(__fdiv_rn(a, b.x), __fdiv_rn(a, b.y)); }
+
+// v = (vx, vy, vz) and its negation nv, so that every c_k . v is the scalar
+// dot_c's sum: a leading negative term is read from nv, a later one is a
+// subtraction (x + (-y) and x - y are the same IEEE operation).
+struct Vel2 {
+    float2 v[3], nv[3];
+};
+template <int Q>
+__device__ __forceinline__ float2 dot_c2(int k, const Vel2& u) {
+    const int c[3] = {Lattice<Q>::cx(k), Lattice<Q>::cy(k), Lattice<Q>::cz(k)};
+    float2 acc = bc2(0.0f);
+    bool any = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (c[a] == 0) continue;
+        if (!any) acc = c[a] > 0 ? u.v[a] : u.nv[a];
+        else acc = c[a] > 0 ? add2(acc, u.v[a]) : sub2(acc, u.v[a]);
+        any = true;
+    }
+    return acc;
+}
+
+// c_k . v for a direction k whose reverse comes after it (k odd): the scalar
+// dot_c's sum, with a leading negative term folded into the following
+// positive one ((-a) + b and b - a are the same IEEE operation); two leading
+// negative terms negate their sum, which can differ from dot_c only in the
+// sign of a zero.
+template <int Q>
+__device__ __forceinline__ float2 dot_c2_fwd(int k, const float2 (&v)[3]) {
+    const int c[3] = {Lattice<Q>::cx(k), Lattice<Q>::cy(k), Lattice<Q>::cz(k)};
+    float2 acc = bc2(0.0f);
+    int n = 0;          // terms summed so far
+    int lead = -1;      // a leading negative term not yet summed
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (c[a] == 0) continue;
+        if (n == 0 && lead < 0 && c[a] < 0) { lead = a; continue; }
+        if (lead >= 0) {
+            acc = c[a] > 0 ? sub2(v[a], v[lead]) : mul2(bc2(-1.0f), add2(v[lead], v[a]));
+            lead = -1;
+            n = 2;
+            continue;
+        }
+        acc = n == 0 ? v[a] : (c[a] > 0 ? add2(acc, v[a]) : sub2(acc, v[a]));
+        ++n;
+    }
+    if (lead >= 0) acc = mul2(bc2(-1.0f), v[lead]);
+    return acc;
+}
+
+template <int Q>
+__device__ __forceinline__ void node_moments_dev2(const float2 (&d)[Q], float2& drho, float2& rho, float2& ux,
+                                                  float2& uy, float2& uz, float2 nz) {
+    float2 r = bc2(0.0f), jx = bc2(0.0f), jy = bc2(0.0f), jz = bc2(0.0f);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        r = add2(r, d[k]);
+        if (Lattice<Q>::cx(k) > 0) jx = add2(jx, d[k]);
+        if (Lattice<Q>::cx(k) < 0) jx = sub2(jx, d[k]);
+        if (Lattice<Q>::cy(k) > 0) jy = add2(jy, d[k]);
+        if (Lattice<Q>::cy(k) < 0) jy = sub2(jy, d[k]);
+        if (Lattice<Q>::cz(k) > 0) jz = add2(jz, d[k]);
+        if (Lattice<Q>::cz(k) < 0) jz = sub2(jz, d[k]);
+    }
+    drho = r;
+    rho = add2(bc2(1.0f), r);
+    const float2 rinv = div2(1.0f, rho);
+    ux = mulx2(jx, rinv, nz);
+    uy = mulx2(jy, rinv, nz);
+    uz = mulx2(jz, rinv, nz);
+}
+
+// collide_node_dev for two nodes
+template <int Q>
+__device__ __forceinline__ void collide_node_dev2(float2 (&d)[Q], float2 drho, float2 rho, float2 ux, float2 uy,
+                                                  float2 uz, const CollideParams& P) {
+    const float2 nz = bc2(P.neg_zero);
+    const float2 tr = div2(P.tau, rho);
+    float2 v[3];
+    v[0] = add2(ux, mulx2(bc2(P.fx), tr, nz));
+    v[1] = add2(uy, mulx2(bc2(P.fy), tr, nz));
+    v[2] = add2(uz, mulx2(bc2(P.fz), tr, nz));
+    const float2 usq = add2(add2(mulx2(v[0], v[0], nz), mulx2(v[1], v[1], nz)), mulx2(v[2], v[2], nz));
+    const float2 kusq = mul2(bc2(-1.5f), usq);
+    const float2 orho = mul2(bc2(P.omega), rho);
+    const float2 odrho = mul2(bc2(P.omega), drho);
+    // c_{k+1} = -c_k for odd k, so the even directions negate the previous
+    // c.v.  A zero's sign cannot reach the result: X = +-0*3 + kusq is kusq,
+    // or +-0 when kusq is -0, and then A X + B is B (B is never -0: the sum
+    // drho starts from +0).
+    float2 cu_prev = bc2(0.0f);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        const float2 cu = (k == 0) ? bc2(0.0f) : ((k & 1) ? dot_c2_fwd<Q>(k, v) : mul2(bc2(-1.0f), cu_prev));
+        cu_prev = cu;
+        const float2 A = mul2(bc2(weight<Q>(k)), orho);
+        const float2 B = mul2(bc2(weight<Q>(k)), odrho);
+        const float2 X = fma2(cu, fma2(bc2(4.5f), cu, bc2(3.0f)), kusq);
+        d[k] = fma2(bc2(P.omc), d[k], fma2(A, X, B));
+    }
+}
+
+// collide_node_trt<Q, true> for two nodes
+template <int Q>
+__device__ __forceinline__ void collide_node_trt_dev2(float2 (&f)[Q], float2 drho, float2 rho, float2 ux, float2 uy,
+                                                      float2 uz, const CollideParams& P) {
+    const float2 nz = bc2(P.neg_zero);
+    const float2 hr = div2(0.5f, rho);
+    Vel2 u;
+    u.v[0] = add2(ux, mulx2(bc2(P.fx), hr, nz));
+    u.v[1] = add2(uy, mulx2(bc2(P.fy), hr, nz));
+    u.v[2] = add2(uz, mulx2(bc2(P.fz), hr, nz));
+#pragma unroll
+    for (int a = 0; a < 3; ++a) u.nv[a] = mul2(bc2(-1.0f), u.v[a]);
+    const float2 vsq =
+        add2(add2(mulx2(u.v[0], u.v[0], nz), mulx2(u.v[1], u.v[1], nz)), mulx2(u.v[2], u.v[2], nz));
+    const float2 uF = add2(add2(mulx2(u.v[0], bc2(P.fx), nz), mulx2(u.v[1], bc2(P.fy), nz)),
+                           mulx2(u.v[2], bc2(P.fz), nz));
+    const float2 kusq = mul2(bc2(-1.5f), vsq);
+    const float2 m3uF = mul2(bc2(-3.0f), uF);
+    const float2 om = bc2(P.omega), omm = bc2(P.omega_m);
+    {
+        const float w0 = weight<Q>(0);
+        const float2 wr0 = mul2(bc2(w0), rho);
+        const float2 e0 = fma2(wr0, kusq, mul2(bc2(w0), drho));
+        f[0] = add2(sub2(f[0], mulx2(om, sub2(f[0], e0), nz)), mulx2(bc2(__fmul_rn(P.gp, w0)), m3uF, nz));
+    }
+#pragma unroll
+    for (int k = 1; k < Q; k += 2) {
+        const float w = weight<Q>(k);
+        const float2 wr = mul2(bc2(w), rho);
+        const float2 cu = dot_c2<Q>(k, u);
+        const float cF = dot_c<Q>(k, P.fx, P.fy, P.fz);
+        const float2 t = mul2(bc2(4.5f), cu);
+        const float2 ep = fma2(wr, fma2(t, cu, kusq), mul2(bc2(w), drho));
+        const float2 em = mulx2(wr, mul2(bc2(3.0f), cu), nz);
+        const float2 sp = mulx2(bc2(0.5f), add2(f[k], f[k + 1]), nz);
+        const float2 sm = mulx2(bc2(0.5f), sub2(f[k], f[k + 1]), nz);
+        const float2 a = mulx2(om, sub2(sp, ep), nz);
+        const float2 b = mulx2(omm, sub2(sm, em), nz);
+        const float2 Sp = mulx2(bc2(__fmul_rn(P.gp, w)), fma2(mul2(bc2(9.0f), cu), bc2(cF), m3uF), nz);
+        const float2 Sm = bc2(__fmul_rn(__fmul_rn(P.gm, w), __fmul_rn(3.0f, cF)));
+        const float2 nk = add2(sub2(sub2(f[k], a), b), add2(Sp, Sm));
+        const float2 nr = add2(add2(sub2(f[k + 1], a), b), sub2(Sp, Sm));
+        f[k] = nk;
+        f[k + 1] = nr;
+    }
+}
+
+// update_node<Q, 1, ARITH> for two nodes
+template <int Q, int ARITH>
+__device__ __forceinline__ void update_pair_dev(float2 (&d)[Q], float2& rho, const CollideParams& cp) {
+    float2 drho, ux, uy, uz;
+    node_moments_dev2<Q>(d, drho, rho, ux, uy, uz, bc2(cp.neg_zero));
+    if constexpr (ARITH == kArithTRT) collide_node_trt_dev2<Q>(d, drho, rho, ux, uy, uz, cp);
+    else collide_node_dev2<Q>(d, drho, rho, ux, uy, uz, cp);
+}
+
 template <int Q, int ST>
 __device__ __forceinline__ void moments_any(const typename Store<ST>::R (&f)[Q], typename Store<ST>::R& rho,
                                             typename Store<ST>::R& ux, typename Store<ST>::R& uy,
@@ -447,30 +647,23 @@ __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, c
         L0 = links_of<MASK>(t0, np.links, node0);
         L1 = links_of<MASK>(t1, np.links, node0 + 1);
     }
-    float f0[Q], f1[Q];
+    float2 f[Q];   // .x node x0, .y node x0 + 1
 #pragma unroll
     for (int k = 0; k < Q; ++k) {
         const int cx = Lattice<Q>::cx(k), cy = Lattice<Q>::cy(k), cz = Lattice<Q>::cz(k);
         const long long row = (long long)k * g.ks + zo[1 - cz] + yo[1 - cy];
-        float lo = 0.0f, hi = 0.0f;
-        if (active) {
-            const __half2 v = __ldg(reinterpret_cast<const __half2*>(src + row + x0));
-            lo = __low2float(v);
-            hi = __high2float(v);
-        }
+        float2 v = make_float2(0.0f, 0.0f);
+        if (active) v = __half22float2(__ldg(reinterpret_cast<const __half2*>(src + row + x0)));
         if (cx == 0) {
-            f0[k] = lo;
-            f1[k] = hi;
+            f[k] = v;
         } else if (cx > 0) {
-            float prev = __shfl_up_sync(kFull, hi, 1);
+            float prev = __shfl_up_sync(kFull, v.y, 1);
             if (edge_lo) prev = (active && xm >= 0) ? __half2float(__ldg(src + row + xm)) : 0.0f;
-            f0[k] = prev;
-            f1[k] = lo;
+            f[k] = make_float2(prev, v.x);
         } else {
-            float next = __shfl_down_sync(kFull, lo, 1);
+            float next = __shfl_down_sync(kFull, v.x, 1);
             if (edge_hi) next = (active && xp2 >= 0) ? __half2float(__ldg(src + row + xp2)) : 0.0f;
-            f0[k] = hi;
-            f1[k] = next;
+            f[k] = make_float2(v.y, next);
         }
     }
     if (skip) return;
@@ -478,35 +671,43 @@ __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, c
 #pragma unroll
         for (int k = 1; k < Q; ++k) {
             const long long slot = (long long)rev_of(k) * g.ks + node0;
-            if ((L0 >> rev_of(k)) & 1u) f0[k] = __half2float(__ldg(src + slot));
-            if ((L1 >> rev_of(k)) & 1u) f1[k] = __half2float(__ldg(src + slot + 1));
+            if ((L0 >> rev_of(k)) & 1u) f[k].x = __half2float(__ldg(src + slot));
+            if ((L1 >> rev_of(k)) & 1u) f[k].y = __half2float(__ldg(src + slot + 1));
         }
     }
-    float rho0, rho1;
-    update_node<Q, 1, ARITH>(f0, rho0, cp);
-    update_node<Q, 1, ARITH>(f1, rho1, cp);
+    float2 rho;
+    update_pair_dev<Q, ARITH>(f, rho, cp);
     if (MASK && MOVING && (L0 | L1)) {
         const Nbr n0(g, x0, y, z), n1(g, x0 + 1, y, z);
 #pragma unroll
         for (int k = 1; k < Q; ++k) {
             if ((L0 >> k) & 1u)
-                f0[k] = wall_corrected<Q, 1>(k, f0[k], rho0, np.vel[__ldg(types + n0.at<Q>(k, +1)) & kVelMask],
-                                             np.cs2inv);
+                f[k].x = wall_corrected<Q, 1>(k, f[k].x, rho.x, np.vel[__ldg(types + n0.at<Q>(k, +1)) & kVelMask],
+                                              np.cs2inv);
             if ((L1 >> k) & 1u)
-                f1[k] = wall_corrected<Q, 1>(k, f1[k], rho1, np.vel[__ldg(types + n1.at<Q>(k, +1)) & kVelMask],
-                                             np.cs2inv);
+                f[k].y = wall_corrected<Q, 1>(k, f[k].y, rho.y, np.vel[__ldg(types + n1.at<Q>(k, +1)) & kVelMask],
+                                              np.cs2inv);
         }
     }
 #pragma unroll
     for (int k = 0; k < Q; ++k) {
-        const __half2 v = __floats2half2_rn(f0[k], f1[k]);
+        const __half2 v = __float22half2_rn(f[k]);
         __stcs(reinterpret_cast<unsigned int*>(dst + (long long)k * g.ks + node0),
                *reinterpret_cast<const unsigned int*>(&v));
     }
 }
 
+// Resident blocks of BX threads the pair kernel is compiled for: 64
+// registers a thread for D3Q19 and D2Q9, 80 for D3Q27 (32 and 24 warps an
+// SM).  Without the bound the compiler takes 70-96, and the warps lost cost
+// more than the spills it avoids; the moving-wall variants keep their own.
+template <int Q, bool MOVING, int BX>
+constexpr int h2_min_blocks() {
+    return MOVING ? 1 : (Q == 27 ? 24 : 32) * 32 / BX;
+}
+
 template <int Q, bool MASK, bool MOVING, int ARITH, int BX>
-__global__ void __launch_bounds__(BX)
+__global__ void __launch_bounds__(BX, (h2_min_blocks<Q, MOVING, BX>()))
 nat_fused_h2_k(Geo g, CollideParams cp, NativeParams np, const __half* __restrict__ src, __half* __restrict__ dst,
                const uint8_t* __restrict__ types) {
     const int lane = threadIdx.x & 31;   // a warp is 32 consecutive pairs of one row
