@@ -203,6 +203,24 @@ int plb_synchronize(plb_solve* s);
  * work after plb_step_async. */
 void* plb_stream_handle(plb_solve* s);
 
+/* ---- kernel autotuning ----------------------------------------------------------
+ * The FP16 pair kernel (NATIVE semantics, FP16 storage, even nx) comes in
+ * several compiled variants that give bit-identical results.  Before a
+ * solve's first fused step the library times each on the solve's own buffers
+ * (the trial steps write only the buffer the next step overwrites) and keeps
+ * the fastest per lattice, storage, collision, mask, block width and size
+ * class (floor(log2 cells)) for the process; PLB_TUNE_CACHE=<file> keeps the
+ * table across processes, PLB_TUNE=0 uses variant 0.  No plbpd counterpart:
+ * plbpd's TBB loops have no launch configuration to tune. */
+/* Number of variants the library compiles (valid ids are 0 .. n-1). */
+int plb_tune_variants(void);
+/* variant >= 0: every solve that has not chosen yet uses it (solves whose
+ * kernel has fewer variants use 0); -1: tune (the default).  PLB_EINVAL
+ * for other values. */
+int plb_tune_force(int32_t variant);
+/* The variant the solve runs, or -1 before its first fused step. */
+int plb_tune_variant(const plb_solve* s, int32_t* variant);
+
 /* ---- batches of solves --------------------------------------------------------
  * A batch advances many NATIVE solves of one lattice, storage and device
  * together: every time step is one launch of a persistent-grid kernel whose

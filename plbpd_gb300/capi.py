@@ -60,6 +60,9 @@ _SIGS = [
     ("plb_step_async", C.c_int, [C.c_void_p, C.c_int64]),
     ("plb_synchronize", C.c_int, [C.c_void_p]),
     ("plb_stream_handle", C.c_void_p, [C.c_void_p]),
+    ("plb_tune_variants", C.c_int, []),
+    ("plb_tune_force", C.c_int, [C.c_int32]),
+    ("plb_tune_variant", C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     ("plb_collide", C.c_int, [C.c_void_p]),
     ("plb_stream_push", C.c_int, [C.c_void_p]),
     ("plb_apply_noslip", C.c_int, [C.c_void_p]),
@@ -226,6 +229,13 @@ class Solve:
     def step_async(self, n: int = 1) -> None: check(lib().plb_step_async(self.h, int(n)))
     def synchronize(self) -> None: check(lib().plb_synchronize(self.h))
     def stream(self) -> int: return lib().plb_stream_handle(self.h) or 0
+
+    def variant(self) -> int:
+        """The fused-step kernel variant the autotuner chose (-1 before the
+        first fused step)."""
+        v = C.c_int32()
+        check(lib().plb_tune_variant(self.h, C.byref(v)))
+        return v.value
     def collide(self) -> None: check(lib().plb_collide(self.h))
     def stream_push(self) -> None: check(lib().plb_stream_push(self.h))
     def apply_noslip(self) -> None: check(lib().plb_apply_noslip(self.h))
@@ -317,6 +327,16 @@ class Batch:
 class Request(C.Structure):
     """plb_request: one solve for the server."""
     _fields_ = [("params", Params), ("mask", C.c_void_p), ("steps", C.c_int64)]
+
+
+def tune_variants() -> int:
+    """Number of compiled variants of the fused-step kernel."""
+    return lib().plb_tune_variants()
+
+
+def tune_force(variant: int) -> None:
+    """Fixes the kernel variant of solves that have not chosen yet (-1: tune)."""
+    check(lib().plb_tune_force(int(variant)))
 
 
 class Server:

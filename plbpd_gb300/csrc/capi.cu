@@ -1,10 +1,16 @@
 // The C ABI (include/plb.h): handle lifetime, validation, state tracking,
 // step orchestration (CUDA-graph chunks of fused steps) and transfers between
 // host buffers in plbpd's layout and the device layout.
+#include <array>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -140,6 +146,8 @@ struct plb_solve {
     int graph_steps = 64;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int64_t device_bytes = 0;
+    // variant of the fused-step kernel (autotuner); -1 until chosen
+    int variant = -1;
 };
 
 namespace {
@@ -395,6 +403,129 @@ int ref_materialize_fields(plb_solve* s) {
     return PLB_OK;
 }
 
+// ---- autotuner of the fused-step kernel --------------------------------------
+// The FP16 pair kernel is compiled in several variants that give the same
+// bits (native_impl.cuh, kH2Variant); which is fastest depends on the
+// lattice, the mask, the block width and the domain size.  Before a solve's
+// first fused step the variants are timed on the solve's own buffers: a pull
+// step reads buffer cur and writes the other one, which the next real step
+// overwrites, so trial launches leave the state as it was.  The winner is
+// kept per (lattice, storage, arithmetic, mask, moving walls, block width,
+// size class = floor(log2 cells)) for the process, and in the file named by
+// PLB_TUNE_CACHE across processes.  PLB_TUNE=0 turns tuning off (variant 0);
+// plb_tune_force fixes one variant.
+using TuneKey = std::array<int, 7>;
+std::mutex g_tune_mu;
+std::map<TuneKey, int> g_tune;
+bool g_tune_loaded = false;
+std::atomic<int> g_tune_force{-1};
+
+std::string device_tag() {
+    int dev = 0;
+    cudaDeviceProp prop{};
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return "unknown";
+    std::string n = prop.name;
+    for (char& c : n)
+        if (c == ' ') c = '_';
+    return n + "_sm" + std::to_string(prop.multiProcessorCount);
+}
+
+// Loads PLB_TUNE_CACHE once (lines: plb-tune-v2 device q storage arith mask
+// moving wide size_class variant); caller holds g_tune_mu.
+void tune_load_locked() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char* path = std::getenv("PLB_TUNE_CACHE");
+    if (!path || !*path) return;
+    std::ifstream in(path);
+    const std::string dev = device_tag();
+    std::string line;
+    while (std::getline(in, line)) {
+        std::istringstream ls(line);
+        std::string magic, d;
+        TuneKey k{};
+        int v = -1;
+        if (!(ls >> magic >> d) || magic != "plb-tune-v2" || d != dev) continue;
+        bool ok = true;
+        for (int& x : k) ok = ok && static_cast<bool>(ls >> x);
+        if (ok && (ls >> v) && v >= 0) g_tune[k] = v;
+    }
+}
+
+void tune_store_locked(const TuneKey& k, int v) {
+    g_tune[k] = v;
+    const char* path = std::getenv("PLB_TUNE_CACHE");
+    if (!path || !*path) return;
+    std::ofstream out(path, std::ios::app);
+    out << "plb-tune-v2 " << device_tag();
+    for (int x : k) out << ' ' << x;
+    out << ' ' << v << '\n';
+}
+
+int fused_variants(const plb_solve* s) {
+    if (!s->native || s->aa) return 1;
+    return nat_fused_variants(s->q, s->storage, s->karith, s->has_mask && s->np.moving, s->g);
+}
+
+int launch_fused(plb_solve* s, int variant) {
+    PLB_KERNEL(nat_fused_step(s->q, s->storage, s->karith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
+                              s->f[1 - s->cur], s->types, variant, s->stream));
+    return PLB_OK;
+}
+
+// Mean time of `reps` launches of one variant, in ms.
+int time_variant(plb_solve* s, int v, int reps, cudaEvent_t e0, cudaEvent_t e1, float* ms) {
+    for (int i = 0; i < 2; ++i) PLB_TRY(launch_fused(s, v));
+    PLB_CUDA(cudaEventRecord(e0, s->stream));
+    for (int i = 0; i < reps; ++i) PLB_TRY(launch_fused(s, v));
+    PLB_CUDA(cudaEventRecord(e1, s->stream));
+    PLB_CUDA(cudaEventSynchronize(e1));
+    PLB_CUDA(cudaEventElapsedTime(ms, e0, e1));
+    *ms /= (float)reps;
+    return PLB_OK;
+}
+
+// Sets s->variant (not during a graph capture: the trials synchronise).
+int choose_variant(plb_solve* s) {
+    const int nv = fused_variants(s);
+    const int forced = g_tune_force.load();
+    if (nv <= 1) { s->variant = 0; return PLB_OK; }
+    if (forced >= 0) { s->variant = forced < nv ? forced : 0; return PLB_OK; }
+    const char* on = std::getenv("PLB_TUNE");
+    if (on && std::strcmp(on, "0") == 0) { s->variant = 0; return PLB_OK; }
+    const long long cells = (long long)s->g.nx * s->g.ny * s->g.nz;
+    int cls = 0;
+    while ((2LL << cls) <= cells) ++cls;
+    const TuneKey key = {s->q, s->storage, s->karith, (int)s->has_mask, (int)(s->has_mask && s->np.moving),
+                         (int)(s->g.nx % 256 == 0), cls};
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        tune_load_locked();
+        auto it = g_tune.find(key);
+        if (it != g_tune.end() && it->second < nv) { s->variant = it->second; return PLB_OK; }
+    }
+    // about 2^25 node updates a trial, 3 to 50 launches
+    const long long r = (1LL << 25) / (cells > 0 ? cells : 1);
+    const int reps = r < 3 ? 3 : (r > 50 ? 50 : (int)r);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    PLB_CUDA(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return fail(PLB_ECUDA, "cudaEventCreate"); }
+    int best = 0, rc = PLB_OK;
+    float best_ms = 0.0f;
+    for (int v = 0; v < nv && rc == PLB_OK; ++v) {
+        float ms = 0.0f;
+        rc = time_variant(s, v, reps, e0, e1, &ms);
+        if (rc == PLB_OK && (v == 0 || ms < best_ms)) { best = v; best_ms = ms; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != PLB_OK) return rc;
+    s->variant = best;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_store_locked(key, best);
+    return PLB_OK;
+}
+
 // ---- NATIVE semantics ------------------------------------------------------
 int nat_one_step(plb_solve* s) {
     if (s->aa) {
@@ -403,8 +534,8 @@ int nat_one_step(plb_solve* s) {
         s->swapped = !s->swapped;
         return PLB_OK;
     }
-    PLB_KERNEL(nat_fused_step(s->q, s->storage, s->karith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
-                              s->f[1 - s->cur], s->types, s->stream));
+    if (s->variant < 0) PLB_TRY(choose_variant(s));
+    PLB_TRY(launch_fused(s, s->variant));
     s->cur = 1 - s->cur;
     return PLB_OK;
 }
@@ -470,6 +601,7 @@ int run_chunk(plb_solve* s) {
     // a chunk has an even number of steps, so it ends in the state it began
     const int parity = s->aa ? (int)s->swapped : s->cur;
     if (!s->graph[parity]) {
+        if (s->native && s->variant < 0) PLB_TRY(choose_variant(s));   // before the capture
         PLB_TRY(capture_chunk(s, parity));   // capture toggles cur an even number of times
     }
     PLB_CUDA(cudaGraphLaunch(s->graph[parity], s->stream));
@@ -741,6 +873,20 @@ int plb_step_async(plb_solve* s, int64_t nsteps) {
     return march(s, nsteps);
 }
 
+int plb_tune_variants(void) { return kFusedVariants; }
+
+int plb_tune_force(int32_t variant) {
+    if (variant < -1 || variant >= kFusedVariants) return fail(PLB_EINVAL, "variant out of range");
+    g_tune_force.store(variant);
+    return PLB_OK;
+}
+
+int plb_tune_variant(const plb_solve* s, int32_t* variant) {
+    if (!s || !variant) return fail(PLB_EINVAL, "null argument");
+    *variant = s->variant;
+    return PLB_OK;
+}
+
 int plb_step(plb_solve* s, int64_t nsteps) {
     PLB_TRY(plb_step_async(s, nsteps));
     return sync(s);
@@ -995,7 +1141,7 @@ int batch_prepare(plb_batch* b, int64_t* consumed) {
             s->post = true;
         } else {
             PLB_KERNEL(nat_fused_step(s->q, s->storage, s->karith, s->has_mask, s->g, s->cp, s->np, s->f[s->cur],
-                                      s->f[1 - s->cur], s->types, b->stream));
+                                      s->f[1 - s->cur], s->types, s->variant < 0 ? 0 : s->variant, b->stream));
         }
         s->cur = 1 - s->cur;
     }

@@ -72,10 +72,24 @@ int nat_collide_raw(int q, int storage, int arith, bool has_mask, const Geo& g,
                     const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
                     const float* rho, const float* u, const uint8_t* types, cudaStream_t st);
 // One fused step: gather P from `src` (streaming + bounce-back), moments,
-// collision, store P into `dst`.
+// collision, store P into `dst`.  `variant` picks among the FP16 pair
+// kernel's compiled variants (all give the same bits); other kernels have one.
 int nat_fused_step(int q, int storage, int arith, bool has_mask, const Geo& g,
                    const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
-                   const uint8_t* types, cudaStream_t st);
+                   const uint8_t* types, int variant, cudaStream_t st);
+// How many variants nat_fused_step has for a configuration (1 unless FP16
+// storage with even nx takes the pair kernel).
+int nat_fused_variants(int q, int storage, int arith, bool moving, const Geo& g);
+// The most variants any configuration has.
+constexpr int kFusedVariants = 7;
+// The BGK pair-kernel step of one lattice (kernels_h2_q<Q>.cu: one file per
+// lattice, so their variants compile in parallel).
+int nat_fused_h2_bgk9(bool mask, const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src,
+                      void* dst, const uint8_t* types, int variant, cudaStream_t st);
+int nat_fused_h2_bgk19(bool mask, const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src,
+                       void* dst, const uint8_t* types, int variant, cudaStream_t st);
+int nat_fused_h2_bgk27(bool mask, const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src,
+                       void* dst, const uint8_t* types, int variant, cudaStream_t st);
 // Gather only: writes n (storage format, or nullptr) and the moments with the
 // solid-node resets (rho/u, or nullptr).
 int nat_gather(int q, int storage, bool has_mask, const Geo& g, const NativeParams& np,

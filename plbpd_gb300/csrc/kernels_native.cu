@@ -88,11 +88,17 @@ nat_reset_fields_k(Geo g, NativeParams np, const uint8_t* __restrict__ types, fl
 }  // namespace
 
 int nat_fused_step(int q, int storage, int arith, bool has_mask, const Geo& g, const CollideParams& cp,
-                   const NativeParams& np, const void* src, void* dst, const uint8_t* types, cudaStream_t st) {
+                   const NativeParams& np, const void* src, void* dst, const uint8_t* types, int variant,
+                   cudaStream_t st) {
     if (arith == kArithTRT) return nat_fused_step_trt(q, storage, has_mask, g, cp, np, src, dst, types, st);
-#define CALL(Q) fused_q<false, Q>(storage, arith, has_mask, g, cp, np, src, dst, types, st)
+#define CALL(Q) fused_q<false, Q>(storage, arith, has_mask, g, cp, np, src, dst, types, variant, st)
     return PLB_Q_DISPATCH(q, CALL);
 #undef CALL
+}
+
+int nat_fused_variants(int q, int storage, int arith, bool moving, const Geo& g) {
+    if (storage != 1 || g.nx % 2 != 0) return 1;
+    return nat_h2_variant_count(q, arith, moving);
 }
 
 int nat_collide_raw(int q, int storage, int arith, bool has_mask, const Geo& g, const CollideParams& cp,

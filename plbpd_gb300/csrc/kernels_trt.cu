@@ -6,7 +6,7 @@ namespace plb {
 
 int nat_fused_step_trt(int q, int storage, bool has_mask, const Geo& g, const CollideParams& cp,
                        const NativeParams& np, const void* src, void* dst, const uint8_t* types, cudaStream_t st) {
-#define CALL(Q) fused_q<true, Q>(storage, kArithTRT, has_mask, g, cp, np, src, dst, types, st)
+#define CALL(Q) fused_q<true, Q>(storage, kArithTRT, has_mask, g, cp, np, src, dst, types, 0, st)
     return PLB_Q_DISPATCH(q, CALL);
 #undef CALL
 }

@@ -402,16 +402,23 @@ __device__ __forceinline__ void node_moments_dev2(const float2 (&d)[Q], float2& 
     uz = mulx2(jz, rinv, nz);
 }
 
-// collide_node_dev for two nodes
-template <int Q>
+// collide_node_dev for two nodes.  NEG selects how c.v is formed: from v
+// and -v for every direction (0), or for an even direction as the negated
+// previous one (1); the two give the same bits and differ in registers.
+template <int Q, bool NEG>
 __device__ __forceinline__ void collide_node_dev2(float2 (&d)[Q], float2 drho, float2 rho, float2 ux, float2 uy,
                                                   float2 uz, const CollideParams& P) {
     const float2 nz = bc2(P.neg_zero);
     const float2 tr = div2(P.tau, rho);
-    float2 v[3];
+    Vel2 u;
+    float2 (&v)[3] = u.v;
     v[0] = add2(ux, mulx2(bc2(P.fx), tr, nz));
     v[1] = add2(uy, mulx2(bc2(P.fy), tr, nz));
     v[2] = add2(uz, mulx2(bc2(P.fz), tr, nz));
+    if (!NEG) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) u.nv[a] = mul2(bc2(-1.0f), v[a]);
+    }
     const float2 usq = add2(add2(mulx2(v[0], v[0], nz), mulx2(v[1], v[1], nz)), mulx2(v[2], v[2], nz));
     const float2 kusq = mul2(bc2(-1.5f), usq);
     const float2 orho = mul2(bc2(P.omega), rho);
@@ -423,7 +430,10 @@ __device__ __forceinline__ void collide_node_dev2(float2 (&d)[Q], float2 drho, f
     float2 cu_prev = bc2(0.0f);
 #pragma unroll
     for (int k = 0; k < Q; ++k) {
-        const float2 cu = (k == 0) ? bc2(0.0f) : ((k & 1) ? dot_c2_fwd<Q>(k, v) : mul2(bc2(-1.0f), cu_prev));
+        const float2 cu = (k == 0) ? bc2(0.0f)
+                          : !NEG   ? dot_c2<Q>(k, u)
+                          : (k & 1) ? dot_c2_fwd<Q>(k, v)
+                                    : mul2(bc2(-1.0f), cu_prev);
         cu_prev = cu;
         const float2 A = mul2(bc2(weight<Q>(k)), orho);
         const float2 B = mul2(bc2(weight<Q>(k)), odrho);
@@ -479,13 +489,29 @@ __device__ __forceinline__ void collide_node_trt_dev2(float2 (&f)[Q], float2 drh
     }
 }
 
-// update_node<Q, 1, ARITH> for two nodes
-template <int Q, int ARITH>
+// update_node<Q, 1, ARITH> for two nodes.  FORM 0 and 1: paired, c.v of
+// collide_node_dev2 with NEG = 1 and 0; FORM 2: the scalar update of each
+// node (one instruction stream a node, more instructions, other registers).
+template <int Q, int ARITH, int FORM>
 __device__ __forceinline__ void update_pair_dev(float2 (&d)[Q], float2& rho, const CollideParams& cp) {
+    if constexpr (FORM == 2) {
+        float a[Q], b[Q];
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            a[k] = d[k].x;
+            b[k] = d[k].y;
+        }
+        update_node<Q, 1, ARITH>(a, rho.x, cp);
+        update_node<Q, 1, ARITH>(b, rho.y, cp);
+#pragma unroll
+        for (int k = 0; k < Q; ++k) d[k] = make_float2(a[k], b[k]);
+        return;
+    }
+    constexpr bool NEG = FORM == 0;
     float2 drho, ux, uy, uz;
     node_moments_dev2<Q>(d, drho, rho, ux, uy, uz, bc2(cp.neg_zero));
     if constexpr (ARITH == kArithTRT) collide_node_trt_dev2<Q>(d, drho, rho, ux, uy, uz, cp);
-    else collide_node_dev2<Q>(d, drho, rho, ux, uy, uz, cp);
+    else collide_node_dev2<Q, NEG>(d, drho, rho, ux, uy, uz, cp);
 }
 
 template <int Q, int ST>
@@ -617,7 +643,7 @@ nat_fused_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::
 // it together (the shuffles), lanes past the end of their row with
 // active = false.  A lane's neighbour lane holds the neighbouring pair of the
 // same row unless x0 is 0 or x0 + 2 is nx, which the edge loads cover.
-template <int Q, bool MASK, bool MOVING, int ARITH>
+template <int Q, bool MASK, bool MOVING, int ARITH, int FORM = 0>
 __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, const NativeParams& np,
                                         const __half* __restrict__ src, __half* __restrict__ dst,
                                         const uint8_t* __restrict__ types, int lane, int x0, int y, int z,
@@ -676,7 +702,7 @@ __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, c
         }
     }
     float2 rho;
-    update_pair_dev<Q, ARITH>(f, rho, cp);
+    update_pair_dev<Q, ARITH, FORM>(f, rho, cp);
     if (MASK && MOVING && (L0 | L1)) {
         const Nbr n0(g, x0, y, z), n1(g, x0 + 1, y, z);
 #pragma unroll
@@ -697,22 +723,37 @@ __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, c
     }
 }
 
-// Resident blocks of BX threads the pair kernel is compiled for: 64
-// registers a thread for D3Q19 and D2Q9, 80 for D3Q27 (32 and 24 warps an
-// SM).  Without the bound the compiler takes 70-96, and the warps lost cost
-// more than the spills it avoids; the moving-wall variants keep their own.
-template <int Q, bool MOVING, int BX>
-constexpr int h2_min_blocks() {
-    return MOVING ? 1 : (Q == 27 ? 24 : 32) * 32 / BX;
-}
+// Pair-kernel variants: the same arithmetic and the same bits, compiled
+// differently.  Which is fastest depends on the lattice, the mask, the block
+// width and the domain (the compiler's register allocation and schedule
+// shift with each), so the autotuner in capi.cu times them per lattice and
+// size class.  form: the update's form (update_pair_dev); regs: a register
+// cap per thread, 0 for the compiler's choice.  D2Q9 stays below every cap
+// and has the first three.
+struct H2Variant {
+    int form;
+    int regs;
+};
+constexpr int kH2Variants = kFusedVariants;
+constexpr H2Variant kH2Variant[kH2Variants] = {{0, 0}, {1, 0}, {2, 0}, {0, 72}, {1, 72}, {0, 80}, {1, 80}};
 
-template <int Q, bool MASK, bool MOVING, int ARITH, int BX>
-__global__ void __launch_bounds__(BX, (h2_min_blocks<Q, MOVING, BX>()))
+template <int Q, bool MASK, bool MOVING, int ARITH, int BX, int FORM>
+__global__ void __launch_bounds__(BX)
 nat_fused_h2_k(Geo g, CollideParams cp, NativeParams np, const __half* __restrict__ src, __half* __restrict__ dst,
                const uint8_t* __restrict__ types) {
     const int lane = threadIdx.x & 31;   // a warp is 32 consecutive pairs of one row
     const int x0 = 2 * (blockIdx.x * BX + threadIdx.x);
-    h2_pair<Q, MASK, MOVING, ARITH>(g, cp, np, src, dst, types, lane, x0, blockIdx.y, blockIdx.z, x0 < g.nx);
+    h2_pair<Q, MASK, MOVING, ARITH, FORM>(g, cp, np, src, dst, types, lane, x0, blockIdx.y, blockIdx.z, x0 < g.nx);
+}
+
+// The same kernel with at most NR registers a thread.
+template <int Q, bool MASK, bool MOVING, int ARITH, int BX, int FORM, int NR>
+__global__ void __maxnreg__(NR)
+nat_fused_h2_kr(Geo g, CollideParams cp, NativeParams np, const __half* __restrict__ src, __half* __restrict__ dst,
+                const uint8_t* __restrict__ types) {
+    const int lane = threadIdx.x & 31;
+    const int x0 = 2 * (blockIdx.x * BX + threadIdx.x);
+    h2_pair<Q, MASK, MOVING, ARITH, FORM>(g, cp, np, src, dst, types, lane, x0, blockIdx.y, blockIdx.z, x0 < g.nx);
 }
 
 // First collision from a RAW state: n at the node itself and the rho/u fields.
@@ -1051,18 +1092,50 @@ auto with_storage_arith(int storage, int arith, F&& f) {
     }
 }
 
+// Variants that exist for a kernel: BGK without moving walls has all of
+// kH2Variant (D2Q9 the three without a cap); TRT and moving walls have
+// variant 0.
+template <int Q, int ARITH, bool MOVING>
+constexpr int h2_variants() {
+    return (ARITH == kArithTRT || MOVING) ? 1 : (Q == 9 ? 3 : kH2Variants);
+}
+
+inline int nat_h2_variant_count(int q, int arith, bool moving) {
+    if (arith == kArithTRT || moving) return 1;
+    return q == 9 ? 3 : kH2Variants;
+}
+
 template <int Q, int ARITH, bool MASK>
 int launch_fused_h2(const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
-                    const uint8_t* types, cudaStream_t st) {
+                    const uint8_t* types, int variant, cudaStream_t st) {
+    auto s2 = (const __half*)src;
+    auto d2 = (__half*)dst;
     auto go = [&](auto bxc) {
         constexpr int BX = decltype(bxc)::value;
         const dim3 grid = seg_grid(g, BX, 2);
-        if (MASK && np.moving)
-            nat_fused_h2_k<Q, true, true, ARITH, BX><<<grid, BX, 0, st>>>(g, cp, np, (const __half*)src,
-                                                                            (__half*)dst, types);
-        else
-            nat_fused_h2_k<Q, MASK, false, ARITH, BX><<<grid, BX, 0, st>>>(g, cp, np, (const __half*)src,
-                                                                             (__half*)dst, types);
+        if (MASK && np.moving) {
+            nat_fused_h2_k<Q, true, true, ARITH, BX, 0><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types);
+            return;
+        }
+        static_assert(kH2Variant[1].form == 1 && kH2Variant[2].form == 2 && kH2Variant[3].regs == 72 &&
+                          kH2Variant[4].form == 1 && kH2Variant[5].regs == 80 && kH2Variant[6].form == 1,
+                      "the launches below follow kH2Variant");
+        constexpr int NV = h2_variants<Q, ARITH, false>();
+        const int v = variant < NV ? variant : 0;
+        if constexpr (NV >= 3) {
+            if (v == 1) { nat_fused_h2_k<Q, MASK, false, ARITH, BX, 1><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types); return; }
+            if (v == 2) { nat_fused_h2_k<Q, MASK, false, ARITH, BX, 2><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types); return; }
+        }
+        if constexpr (NV == kH2Variants) {
+            switch (v) {
+                case 3: nat_fused_h2_kr<Q, MASK, false, ARITH, BX, 0, 72><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types); return;
+                case 4: nat_fused_h2_kr<Q, MASK, false, ARITH, BX, 1, 72><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types); return;
+                case 5: nat_fused_h2_kr<Q, MASK, false, ARITH, BX, 0, 80><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types); return;
+                case 6: nat_fused_h2_kr<Q, MASK, false, ARITH, BX, 1, 80><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types); return;
+                default: break;
+            }
+        }
+        nat_fused_h2_k<Q, MASK, false, ARITH, BX, 0><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types);
     };
     if (block_x(g, 2) == kBlockX) go(std::integral_constant<int, kBlockX>{});
     else go(std::integral_constant<int, 32>{});
@@ -1072,13 +1145,20 @@ int launch_fused_h2(const Geo& g, const CollideParams& cp, const NativeParams& n
 // One fused step (FP16 storage with even nx: the pair kernel).
 template <bool TRT, int Q>
 int fused_q(int storage, int arith, bool m, const Geo& g, const CollideParams& cp, const NativeParams& np,
-            const void* src, void* dst, const uint8_t* types, cudaStream_t st) {
+            const void* src, void* dst, const uint8_t* types, int variant, cudaStream_t st) {
     return with_storage_arith<TRT>(storage, arith, [&](auto stc, auto arc) {
         constexpr int ST = decltype(stc)::value, AR = decltype(arc)::value;
         if constexpr (ST == 1) {
-            if (g.nx % 2 == 0)
-                return m ? launch_fused_h2<Q, AR, true>(g, cp, np, src, dst, types, st)
-                         : launch_fused_h2<Q, AR, false>(g, cp, np, src, dst, types, st);
+            if (g.nx % 2 == 0) {
+                if constexpr (TRT) {
+                    return m ? launch_fused_h2<Q, AR, true>(g, cp, np, src, dst, types, 0, st)
+                             : launch_fused_h2<Q, AR, false>(g, cp, np, src, dst, types, 0, st);
+                } else {
+                    if constexpr (Q == 9) return nat_fused_h2_bgk9(m, g, cp, np, src, dst, types, variant, st);
+                    if constexpr (Q == 19) return nat_fused_h2_bgk19(m, g, cp, np, src, dst, types, variant, st);
+                    if constexpr (Q == 27) return nat_fused_h2_bgk27(m, g, cp, np, src, dst, types, variant, st);
+                }
+            }
         }
         return m ? launch_fused<Q, ST, true, AR>(g, cp, np, src, dst, types, st)
                  : launch_fused<Q, ST, false, AR>(g, cp, np, src, dst, types, st);

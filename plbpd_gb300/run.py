@@ -93,7 +93,7 @@ def main(argv=None):
         print(json.dumps({"workload": a.workload, "model": a.model, "dims": [int(p.nx), int(p.ny), int(p.nz)],
                           "storage": a.storage, "arith": a.arith, "spheres": a.spheres, "steps": a.steps,
                           "seconds": round(dt, 4), "mlups": round(cells * a.steps / dt / 1e6, 1),
-                          "mass": s.conservation()[0], "device_bytes": s.device_bytes()}))
+                          "mass": s.conservation()[0], "device_bytes": s.device_bytes(), "variant": s.variant()}))
 
 
 if __name__ == "__main__":

@@ -98,3 +98,15 @@ def test_invalid_parameters_rejected_before_any_device_work(lib):
         with pytest.raises(capi.PlbError) as e:
             capi.Solve.create(**kw)
         assert e.value.code in (capi.EINVAL, capi.EUNSUPPORTED)
+
+
+def test_tune_force_range(lib):
+    from plbpd_gb300 import capi
+    n = capi.tune_variants()
+    assert n >= 1
+    for bad in (-2, n, 1000):
+        with pytest.raises(capi.PlbError) as e:
+            capi.tune_force(bad)
+        assert e.value.code == capi.EINVAL
+    capi.tune_force(0)
+    capi.tune_force(-1)

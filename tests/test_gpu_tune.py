@@ -1,0 +1,72 @@
+"""The fused-step autotuner: every compiled variant of the FP16 pair kernel
+gives the oracle's bits, and a tuned solve runs one of them and records it."""
+import numpy as np
+import pytest
+
+import pyoracle as po
+from test_gpu_native import NATIVE_CASES, compare, mask_for, perturbed_start
+
+pytestmark = pytest.mark.gpu
+
+# even nx (the pair kernel); duct_d3q27 has moving walls (one variant)
+PAIR_CASES = ["torus_d3q19", "obstacles_d3q19", "channel_d2q9", "obstacles_torus_d3q27", "duct_d3q27"]
+
+
+def oracle_after(case, steps):
+    cfg = NATIVE_CASES[case]
+    mask = mask_for(case, cfg)
+    p = po.Port(**cfg, mode=po.MODE_NATIVE, mask=mask, arith=po.ARITH_FP16DEV)
+    p._cfg = cfg
+    p.initialize()
+    start = perturbed_start(p, 11)
+    p.set(po.N, start[0]); p.set(po.RHO, start[1]); p.set(po.U, start[2])
+    p.step(steps)
+    return cfg, mask, start, p
+
+
+def gpu_solve(capi, cfg, mask, start, steps):
+    s = capi.Solve.create(**cfg, semantics=capi.SEMANTICS_NATIVE, storage=capi.STORAGE_FP16_DEV)
+    if mask is not None:
+        s.set_mask(mask)
+    s.initialize()
+    s.set(0, start[0]); s.set(2, start[1]); s.set(3, start[2])
+    s.step(steps)
+    return s
+
+
+@pytest.mark.parametrize("case", PAIR_CASES)
+def test_every_variant_matches_oracle(case):
+    from plbpd_gb300 import capi
+    cfg, mask, start, p = oracle_after(case, 20)
+    try:
+        for v in range(capi.tune_variants()):
+            capi.tune_force(v)
+            with gpu_solve(capi, cfg, mask, start, 20) as s:
+                assert s.variant() in (v, 0)
+                compare(s, p, mask, f"{case} variant {v}")
+    finally:
+        capi.tune_force(-1)
+
+
+def test_tuned_solve_records_its_choice(tmp_path, monkeypatch):
+    from plbpd_gb300 import capi
+    cache = tmp_path / "tune.txt"
+    monkeypatch.setenv("PLB_TUNE_CACHE", str(cache))
+    monkeypatch.delenv("PLB_TUNE", raising=False)
+    # a size class no other test uses, so this solve tunes rather than reuses
+    cfg = dict(NATIVE_CASES["torus_d3q19"], nx=48, ny=40, nz=36)
+    p = po.Port(**cfg, mode=po.MODE_NATIVE, arith=po.ARITH_FP16DEV)
+    p._cfg = cfg
+    p.initialize()
+    start = perturbed_start(p, 5)
+    p.set(po.N, start[0]); p.set(po.RHO, start[1]); p.set(po.U, start[2])
+    p.step(130)
+    with gpu_solve(capi, cfg, None, start, 130) as s:   # a graph chunk and single steps
+        v = s.variant()
+        assert 0 <= v < capi.tune_variants()
+        compare(s, p, None, "tuned")
+    lines = [l.split() for l in cache.read_text().splitlines()]
+    assert lines and lines[-1][0] == "plb-tune-v2" and int(lines[-1][-1]) == v
+    # the same class again takes the recorded choice
+    with gpu_solve(capi, cfg, None, start, 2) as s2:
+        assert s2.variant() == v
