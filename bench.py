@@ -62,48 +62,6 @@ def nu_for_tau(tau: float) -> float:
 
 
 # ---------------------------------------------------------------------------
-# initial state (host, plbpd's layout)
-# ---------------------------------------------------------------------------
-def lattice(q=Q):
-    from plbpd_gb300 import capi
-    c, w, _, _ = capi.model_tables({9: "D2Q9", 19: "D3Q19", 27: "D3Q27"}[q])
-    return c, w
-
-
-def taylor_green_state(n_side: int, out_n=None, out_rho=None, out_u=None):
-    """rho, u and EqlbDist(rho, u) (src/EqlbDist.hpp:26-38 rounding) on the
-    interior of plbpd-layout arrays (nz+2, ny+2, nx+2, V)."""
-    rng = np.random.default_rng(SEED)
-    N = n_side
-    shape3 = (N, N, N)
-    rho = (1.0 + 1e-3 * rng.standard_normal(shape3)).astype(np.float32)
-    ax = 2.0 * np.pi * np.arange(N) / N
-    zc, yc, xc = np.meshgrid(ax, ax, ax, indexing="ij")
-    A = 0.02
-    ux = (A * np.sin(xc) * np.cos(yc) * np.cos(zc) + 1e-4 * rng.standard_normal(shape3)).astype(np.float32)
-    uy = (-A * np.cos(xc) * np.sin(yc) * np.cos(zc) + 1e-4 * rng.standard_normal(shape3)).astype(np.float32)
-    uz = (1e-4 * rng.standard_normal(shape3)).astype(np.float32)
-    del zc, yc, xc
-    full = (N + 2, N + 2, N + 2)
-    n_arr = out_n if out_n is not None else np.zeros(full + (Q,), np.float32)
-    r_arr = out_rho if out_rho is not None else np.zeros(full + (1,), np.float32)
-    u_arr = out_u if out_u is not None else np.zeros(full + (3,), np.float32)
-    r_arr[1:-1, 1:-1, 1:-1, 0] = rho
-    u_arr[1:-1, 1:-1, 1:-1, 0] = ux
-    u_arr[1:-1, 1:-1, 1:-1, 1] = uy
-    u_arr[1:-1, 1:-1, 1:-1, 2] = uz
-    c, w = lattice()
-    usq = (ux * ux + uy * uy) + uz * uz
-    for k in range(Q):
-        cu = (np.float32(c[k, 0]) * ux + np.float32(c[k, 1]) * uy) + np.float32(c[k, 2]) * uz
-        wr = (w[k] * rho).astype(np.float64)
-        cud = cu.astype(np.float64)
-        br = 1.0 + 3.0 * cud + 4.5 * cud * cud - 1.5 * usq.astype(np.float64)
-        n_arr[1:-1, 1:-1, 1:-1, k] = (wr * br).astype(np.float32)
-    return n_arr, r_arr, u_arr
-
-
-# ---------------------------------------------------------------------------
 # clocks during a timed region
 # ---------------------------------------------------------------------------
 class ClockSampler:
@@ -321,7 +279,8 @@ def run_gpu_arm(args):
     pin_u = capi.PinnedBuffer(full + (3,))
     out_rho = capi.PinnedBuffer(full + (1,))
     out_u = capi.PinnedBuffer(full + (3,))
-    taylor_green_state(N_SIDE, pin_n.array, pin_rho.array, pin_u.array)
+    from plbpd_gb300.workloads import taylor_green_state
+    taylor_green_state(N_SIDE, pin_n.array, pin_rho.array, pin_u.array, seed=SEED)
 
     s = capi.Solve(params)
     stream = torch.cuda.ExternalStream(s.stream(), device=torch.device("cuda", local))

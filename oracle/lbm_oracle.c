@@ -154,6 +154,8 @@ float orc_round_half(float f) {
     return r;
 }
 
+float orc_store_half(float d) { return orc_round_half(d * 4096.0f) * (1.0f / 4096.0f); }
+
 /* ---- two instantiations ----------------------------------------------------- */
 #define R float
 #define FN(x) x##_f
@@ -374,7 +376,7 @@ void orc_set_field(orc_sim* s, int which, const float* in) {
         float* d = (float*)p;
         for (size_t i = 0; i < len; ++i) {
             const float v = in[i] - s->w[i % (size_t)s->q];
-            d[i] = s->arith == ORC_ARITH_FP16DEV ? orc_round_half(v) : v;
+            d[i] = s->arith == ORC_ARITH_FP16DEV ? orc_store_half(v) : v;
         }
         return;
     }

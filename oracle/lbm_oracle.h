@@ -120,6 +120,10 @@ void orc_relaxation(const orc_sim* s, float* tau, float* omega);
  * returned as a float. */
 float orc_round_half(float f);
 
+/* The value FP16 storage keeps of a deviation d = f - w: the engine stores
+ * binary16(d * 2^12) and reads it back times 2^-12 (both scalings exact). */
+float orc_store_half(float d);
+
 /* Sum over fluid interior nodes of n_k and n_k c_k, in double:
  * out[0] = mass, out[1..3] = momentum. */
 void orc_conservation(const orc_sim* s, double* out);

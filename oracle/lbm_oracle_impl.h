@@ -169,8 +169,9 @@ static void FN(collide)(orc_sim* s) {
             }
 }
 
-/* FP16 storage: every fluid population rounds to binary16 once per step,
- * after the bounce-back writes (the engine rounds when it stores). */
+/* FP16 storage: every fluid population rounds to the stored binary16 value
+ * (orc_store_half) once per step, after the bounce-back writes (the engine
+ * rounds when it stores). */
 static void FN(quantize)(orc_sim* s) {
 #if ORC_IS_DOUBLE
     (void)s;
@@ -184,7 +185,7 @@ static void FN(quantize)(orc_sim* s) {
             for (long x = 1; x <= s->nx; ++x) {
                 const size_t i = FN(node)(s, z, y, x);
                 if (s->solid[i]) continue;
-                for (int k = 0; k < q; ++k) n[i * q + k] = orc_round_half(n[i * q + k]);
+                for (int k = 0; k < q; ++k) n[i * q + k] = orc_store_half(n[i * q + k]);
             }
 #endif
 }
@@ -422,7 +423,7 @@ static void FN(init_fields)(orc_sim* s) {
     if (orc_dev(s))
         for (int k = 0; k < s->q; ++k) {
             feq[k] = feq[k] - s->w[k];
-            if (s->arith == ORC_ARITH_FP16DEV) feq[k] = orc_round_half(feq[k]);
+            if (s->arith == ORC_ARITH_FP16DEV) feq[k] = orc_store_half(feq[k]);
         }
 #endif
     for (size_t i = 0; i < cells; ++i) {

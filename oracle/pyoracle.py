@@ -70,6 +70,10 @@ def _load_port() -> C.CDLL:
     lib.orc_model_tables.argtypes = [C.c_int, _ip, _fp, C.POINTER(C.c_uint32), _fp]
     lib.orc_model_tables.restype = C.c_int
     lib.orc_set_threads.argtypes = [C.c_int]
+    lib.orc_round_half.argtypes = [C.c_float]
+    lib.orc_round_half.restype = C.c_float
+    lib.orc_store_half.argtypes = [C.c_float]
+    lib.orc_store_half.restype = C.c_float
     lib.orc_max_threads.restype = C.c_int
     return lib
 

@@ -24,8 +24,8 @@ __global__ void init_uniform_k(Geo g, int q, const float* __restrict__ feq, cons
             static_cast<float*>(n)[k * g.ks + i] = feq[k];
             if (nt) static_cast<float*>(nt)[k * g.ks + i] = 0.0f;
         } else if (ST == 1) {
-            static_cast<__half*>(n)[k * g.ks + i] = __float2half_rn(__fsub_rn(feq[k], wk[k]));
-            if (nt) static_cast<__half*>(nt)[k * g.ks + i] = __float2half_rn(-wk[k]);
+            static_cast<__half*>(n)[k * g.ks + i] = __float2half_rn(__fmul_rn(__fsub_rn(feq[k], wk[k]), kHalfScale));
+            if (nt) static_cast<__half*>(nt)[k * g.ks + i] = __float2half_rn(__fmul_rn(-wk[k], kHalfScale));
         } else if (ST == 3) {
             static_cast<float*>(n)[k * g.ks + i] = __fsub_rn(feq[k], wk[k]);
             if (nt) static_cast<float*>(nt)[k * g.ks + i] = -wk[k];
@@ -54,7 +54,9 @@ __global__ void export_k(Geo g, int v, const void* __restrict__ src, const float
         float val = 0.0f;
         if (held) {
             if (ST == 0) val = static_cast<const float*>(src)[c * g.ks + node];
-            else if (ST == 1) val = __fadd_rn(__half2float(static_cast<const __half*>(src)[c * g.ks + node]), wk[c]);
+            else if (ST == 1)
+                val = __fadd_rn(__fmul_rn(__half2float(static_cast<const __half*>(src)[c * g.ks + node]), kHalfUnscale),
+                                wk[c]);
             else if (ST == 3) val = __fadd_rn(static_cast<const float*>(src)[c * g.ks + node], wk[c]);
             else val = __double2float_rn(static_cast<const double*>(src)[c * g.ks + node]);
         }
@@ -76,7 +78,8 @@ __global__ void import_k(Geo g, int v, const float* __restrict__ aos, const floa
     for (int c = 0; c < v; ++c) {
         const float val = aos[i * v + c];
         if (ST == 0) static_cast<float*>(dst)[c * g.ks + node] = val;
-        else if (ST == 1) static_cast<__half*>(dst)[c * g.ks + node] = __float2half_rn(__fsub_rn(val, wk[c]));
+        else if (ST == 1)
+            static_cast<__half*>(dst)[c * g.ks + node] = __float2half_rn(__fmul_rn(__fsub_rn(val, wk[c]), kHalfScale));
         else if (ST == 3) static_cast<float*>(dst)[c * g.ks + node] = __fsub_rn(val, wk[c]);
         else static_cast<double*>(dst)[c * g.ks + node] = (double)val;
     }
@@ -111,7 +114,9 @@ conservation_k(Geo g, const void* __restrict__ n, const uint8_t* __restrict__ ty
         for (int k = 0; k < Q; ++k) {
             double v;
             if (ST == 0) v = (double)static_cast<const float*>(n)[k * g.ks + node];
-            else if (ST == 1) v = (double)__half2float(static_cast<const __half*>(n)[k * g.ks + node]) + (double)weight<Q>(k);
+            else if (ST == 1)
+                v = (double)__fmul_rn(__half2float(static_cast<const __half*>(n)[k * g.ks + node]), kHalfUnscale) +
+                    (double)weight<Q>(k);
             else if (ST == 3) v = (double)static_cast<const float*>(n)[k * g.ks + node] + (double)weight<Q>(k);
             else v = static_cast<const double*>(n)[k * g.ks + node];
             m += v;

@@ -137,6 +137,18 @@ struct CollideParams {
     float neg_zero = -0.0f;
 };
 
+// FP16 storage holds h = binary16(d * 2^12), d = f - w.  The power-of-2
+// scale is exact both ways and moves binary16's normal range (down to
+// 6.1e-5) to 1.5e-8 in d, so the small deviations of slow flows keep all 11
+// bits instead of falling into subnormals; |d| must stay below 16.
+constexpr int kHalfShift = 12;
+constexpr float kHalfScale = 4096.0f;
+constexpr float kHalfUnscale = 1.0f / 4096.0f;
+
+// 2^sc and 2^-sc for the deviation arithmetic's scale (0 or kHalfShift).
+__host__ __device__ constexpr float pow2f(int sc) { return sc == 0 ? 1.0f : sc == kHalfShift ? kHalfScale : 0.0f; }
+__host__ __device__ constexpr float pow2f_neg(int sc) { return sc == 0 ? 1.0f : sc == kHalfShift ? kHalfUnscale : 0.0f; }
+
 // Kernel arithmetic: plbpd's (FP32 body + FP64 tail), FP32 only, or the
 // two-relaxation-time operator (FP32 arithmetic).
 enum Arith : int { kArithReference = 0, kArithFP32 = 1, kArithTRT = 2 };
@@ -216,9 +228,15 @@ __device__ __forceinline__ float dot_c(int k, float ux, float uy, float uz) {
 //     e- = (w rho)(3 cu); s+ = 0.5 (nk + nr); s- = 0.5 (nk - nr)
 //     a = om (s+ - e+); b = omm (s- - e-); S+ = (gp w) fma(9 cu, cF, m3uF); S- = (gm w)(3 cF)
 //     nk = ((nk - a) - b) + (S+ + S-); nr = ((nr - a) + b) + (S+ - S-)
-template <int Q, bool DEV>
+//
+// SC: the populations (and drho) are deviations times 2^SC (FP16 storage
+// keeps them so).  Every term is then the unscaled one times 2^SC: the
+// weights that multiply rho, gp w and gm w carry the factor, which is exact,
+// so the result is the unscaled operator's, times 2^SC, bit for bit.
+template <int Q, bool DEV, int SC = 0>
 __device__ __forceinline__ void collide_node_trt(float (&f)[Q], float drho, float rho, float ux, float uy, float uz,
                                                  const CollideParams& P) {
+    constexpr float S = pow2f(SC);
     const float hr = __fdiv_rn(0.5f, rho);
     const float vx = __fadd_rn(ux, __fmul_rn(P.fx, hr));
     const float vy = __fadd_rn(uy, __fmul_rn(P.fy, hr));
@@ -230,13 +248,14 @@ __device__ __forceinline__ void collide_node_trt(float (&f)[Q], float drho, floa
     const float m3uF = __fmul_rn(-3.0f, uF);
     const float om = P.omega, omm = P.omega_m;
     {
-        const float w0 = weight<Q>(0), wr0 = __fmul_rn(w0, rho);
+        const float w0 = weight<Q>(0), wr0 = __fmul_rn(w0 * S, rho);
         const float e0 = DEV ? __fmaf_rn(wr0, kusq, __fmul_rn(w0, drho)) : __fmul_rn(wr0, base);
-        f[0] = __fadd_rn(__fsub_rn(f[0], __fmul_rn(om, __fsub_rn(f[0], e0))), __fmul_rn(__fmul_rn(P.gp, w0), m3uF));
+        f[0] = __fadd_rn(__fsub_rn(f[0], __fmul_rn(om, __fsub_rn(f[0], e0))),
+                         __fmul_rn(__fmul_rn(__fmul_rn(P.gp, w0), S), m3uF));
     }
 #pragma unroll
     for (int k = 1; k < Q; k += 2) {
-        const float w = weight<Q>(k), wr = __fmul_rn(w, rho);
+        const float w = weight<Q>(k), wr = __fmul_rn(w * S, rho);
         const float cu = dot_c<Q>(k, vx, vy, vz);
         const float cF = dot_c<Q>(k, P.fx, P.fy, P.fz);
         const float t = __fmul_rn(4.5f, cu);
@@ -247,8 +266,8 @@ __device__ __forceinline__ void collide_node_trt(float (&f)[Q], float drho, floa
         const float sm = __fmul_rn(0.5f, __fsub_rn(f[k], f[k + 1]));
         const float a = __fmul_rn(om, __fsub_rn(sp, ep));
         const float b = __fmul_rn(omm, __fsub_rn(sm, em));
-        const float Sp = __fmul_rn(__fmul_rn(P.gp, w), __fmaf_rn(__fmul_rn(9.0f, cu), cF, m3uF));
-        const float Sm = __fmul_rn(__fmul_rn(P.gm, w), __fmul_rn(3.0f, cF));
+        const float Sp = __fmul_rn(__fmul_rn(__fmul_rn(P.gp, w), S), __fmaf_rn(__fmul_rn(9.0f, cu), cF, m3uF));
+        const float Sm = __fmul_rn(__fmul_rn(__fmul_rn(P.gm, w), S), __fmul_rn(3.0f, cF));
         const float nk = __fadd_rn(__fsub_rn(__fsub_rn(f[k], a), b), __fadd_rn(Sp, Sm));
         const float nr = __fadd_rn(__fadd_rn(__fsub_rn(f[k + 1], a), b), __fsub_rn(Sp, Sm));
         f[k] = nk;

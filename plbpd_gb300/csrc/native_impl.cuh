@@ -60,6 +60,7 @@ template <> struct Store<0> {
 template <> struct Store<1> {
     using T = __half;
     using R = float;
+    // the stored value x = 2^12 d; the kernels compute on x (SC = kHalfShift)
     __device__ static __forceinline__ float ld(const __half* p, long long i) { return __half2float(__ldg(p + i)); }
     __device__ static __forceinline__ float ldp(const __half* p, long long i) { return __half2float(p[i]); }
     __device__ static __forceinline__ void st(__half* p, long long i, float v) {
@@ -74,6 +75,10 @@ template <> struct Store<3> {
     __device__ static __forceinline__ float ldp(const float* p, long long i) { return p[i]; }
     __device__ static __forceinline__ void st(float* p, long long i, float v) { __stcs(p + i, v); }
 };
+// The scale of a storage's deviation arithmetic: FP16 computes on 2^12 d.
+template <int ST>
+__host__ __device__ constexpr int dev_shift() { return ST == 1 ? kHalfShift : 0; }
+
 template <> struct Store<2> {
     using T = double;
     using R = double;
@@ -113,7 +118,10 @@ struct Nbr {
 // Written for few operations: per weight class A = w (omega rho) and
 // B = w (omega drho), then per direction
 //   X = fma(cu, fma(4.5, cu, 3), -1.5 usq),  d' = fma(1 - omega, d, fma(A, X, B)).
-template <int Q>
+// SC: d and drho are deviations times 2^SC (FP16 storage keeps x = 2^12 d);
+// A then takes the factor through w 2^SC, B through drho, so every result is
+// the unscaled one times 2^SC, bit for bit (power-of-2 factors are exact).
+template <int Q, int SC = 0>
 __device__ __forceinline__ void collide_node_dev(float (&d)[Q], float drho, float rho, float ux, float uy,
                                                  float uz, const CollideParams& P) {
     const float tr = __fdiv_rn(P.tau, rho);
@@ -127,20 +135,23 @@ __device__ __forceinline__ void collide_node_dev(float (&d)[Q], float drho, floa
 #pragma unroll
     for (int k = 0; k < Q; ++k) {
         const float cu = (k == 0) ? 0.0f : dot_c<Q>(k, vx, vy, vz);
-        const float A = __fmul_rn(weight<Q>(k), orho);     // shared by a weight class after CSE
+        const float A = __fmul_rn(weight<Q>(k) * pow2f(SC), orho);   // shared by a weight class after CSE
         const float B = __fmul_rn(weight<Q>(k), odrho);
         const float X = __fmaf_rn(cu, __fmaf_rn(4.5f, cu, 3.0f), kusq);
         d[k] = __fmaf_rn(P.omc, d[k], __fmaf_rn(A, X, B));
     }
 }
 
-template <int Q>
+// Moments from (scaled) deviations: drho comes back scaled, rho and u do not
+// (rho = 1 + 2^-SC drho and 1/rho 2^-SC are exact rescalings).
+template <int Q, int SC = 0>
 __device__ __forceinline__ void node_moments_dev(const float (&d)[Q], float& drho, float& rho, float& ux,
                                                  float& uy, float& uz) {
     float jx, jy, jz;
     node_sums<Q>(d, drho, jx, jy, jz);
-    rho = __fadd_rn(1.0f, drho);
-    const float rinv = __fdiv_rn(1.0f, rho);
+    rho = SC ? __fmaf_rn(drho, pow2f_neg(SC), 1.0f) : __fadd_rn(1.0f, drho);
+    float rinv = __fdiv_rn(1.0f, rho);
+    if (SC) rinv = __fmul_rn(rinv, pow2f_neg(SC));
     ux = __fmul_rn(jx, rinv);
     uy = __fmul_rn(jy, rinv);
     uz = __fmul_rn(jz, rinv);
@@ -262,12 +273,20 @@ __device__ __forceinline__ void collide_any(typename Store<ST>::R (&f)[Q], typen
     if constexpr (ST == 0) {
         collide_node<Q, ARITH>(f, rho, ux, uy, uz, cp);
     } else if constexpr (ST == 1 || ST == 3) {
-        if constexpr (ARITH == kArithTRT) collide_node_trt<Q, true>(f, drho, rho, ux, uy, uz, cp);
-        else collide_node_dev<Q>(f, drho, rho, ux, uy, uz, cp);
+        if constexpr (ARITH == kArithTRT) collide_node_trt<Q, true, dev_shift<ST>()>(f, drho, rho, ux, uy, uz, cp);
+        else collide_node_dev<Q, dev_shift<ST>()>(f, drho, rho, ux, uy, uz, cp);
     } else {
         if constexpr (ARITH == kArithTRT) collide_node_trt_d<Q>(f, rho, ux, uy, uz, cp);
         else collide_node_d<Q>(f, rho, ux, uy, uz, cp);
     }
+}
+
+// drho of a RAW state's rho field, in the deviation arithmetic's scale.
+template <int ST>
+__device__ __forceinline__ float raw_drho(float rho) {
+    if constexpr (ST == 1) return __fmul_rn(__fsub_rn(rho, 1.0f), kHalfScale);
+    else if constexpr (ST == 3) return __fsub_rn(rho, 1.0f);
+    else return 0.0f;
 }
 
 template <int Q, int ST, int ARITH>
@@ -279,7 +298,7 @@ __device__ __forceinline__ void update_node(typename Store<ST>::R (&f)[Q], typen
         collide_any<Q, ST, ARITH>(f, rho, ux, uy, uz, 0.0f, cp);
     } else if constexpr (ST == 1 || ST == 3) {
         float drho, ux, uy, uz;
-        node_moments_dev<Q>(f, drho, rho, ux, uy, uz);
+        node_moments_dev<Q, dev_shift<ST>()>(f, drho, rho, ux, uy, uz);
         collide_any<Q, ST, ARITH>(f, rho, ux, uy, uz, drho, cp);
     } else {
         double ux, uy, uz;
@@ -380,7 +399,7 @@ __device__ __forceinline__ float2 dot_c2_fwd(int k, const float2 (&v)[3]) {
     return acc;
 }
 
-template <int Q>
+template <int Q, int SC>
 __device__ __forceinline__ void node_moments_dev2(const float2 (&d)[Q], float2& drho, float2& rho, float2& ux,
                                                   float2& uy, float2& uz, float2 nz) {
     float2 r = bc2(0.0f), jx = bc2(0.0f), jy = bc2(0.0f), jz = bc2(0.0f);
@@ -395,8 +414,9 @@ __device__ __forceinline__ void node_moments_dev2(const float2 (&d)[Q], float2& 
         if (Lattice<Q>::cz(k) < 0) jz = sub2(jz, d[k]);
     }
     drho = r;
-    rho = add2(bc2(1.0f), r);
-    const float2 rinv = div2(1.0f, rho);
+    rho = SC ? fma2(r, bc2(pow2f_neg(SC)), bc2(1.0f)) : add2(bc2(1.0f), r);
+    float2 rinv = div2(1.0f, rho);
+    if (SC) rinv = mul2(rinv, bc2(pow2f_neg(SC)));
     ux = mulx2(jx, rinv, nz);
     uy = mulx2(jy, rinv, nz);
     uz = mulx2(jz, rinv, nz);
@@ -405,7 +425,7 @@ __device__ __forceinline__ void node_moments_dev2(const float2 (&d)[Q], float2& 
 // collide_node_dev for two nodes.  NEG selects how c.v is formed: from v
 // and -v for every direction (0), or for an even direction as the negated
 // previous one (1); the two give the same bits and differ in registers.
-template <int Q, bool NEG>
+template <int Q, bool NEG, int SC>
 __device__ __forceinline__ void collide_node_dev2(float2 (&d)[Q], float2 drho, float2 rho, float2 ux, float2 uy,
                                                   float2 uz, const CollideParams& P) {
     const float2 nz = bc2(P.neg_zero);
@@ -435,15 +455,15 @@ __device__ __forceinline__ void collide_node_dev2(float2 (&d)[Q], float2 drho, f
                           : (k & 1) ? dot_c2_fwd<Q>(k, v)
                                     : mul2(bc2(-1.0f), cu_prev);
         cu_prev = cu;
-        const float2 A = mul2(bc2(weight<Q>(k)), orho);
+        const float2 A = mul2(bc2(weight<Q>(k) * pow2f(SC)), orho);
         const float2 B = mul2(bc2(weight<Q>(k)), odrho);
         const float2 X = fma2(cu, fma2(bc2(4.5f), cu, bc2(3.0f)), kusq);
         d[k] = fma2(bc2(P.omc), d[k], fma2(A, X, B));
     }
 }
 
-// collide_node_trt<Q, true> for two nodes
-template <int Q>
+// collide_node_trt<Q, true, SC> for two nodes
+template <int Q, int SC>
 __device__ __forceinline__ void collide_node_trt_dev2(float2 (&f)[Q], float2 drho, float2 rho, float2 ux, float2 uy,
                                                       float2 uz, const CollideParams& P) {
     const float2 nz = bc2(P.neg_zero);
@@ -463,14 +483,15 @@ __device__ __forceinline__ void collide_node_trt_dev2(float2 (&f)[Q], float2 drh
     const float2 om = bc2(P.omega), omm = bc2(P.omega_m);
     {
         const float w0 = weight<Q>(0);
-        const float2 wr0 = mul2(bc2(w0), rho);
+        const float2 wr0 = mul2(bc2(w0 * pow2f(SC)), rho);
         const float2 e0 = fma2(wr0, kusq, mul2(bc2(w0), drho));
-        f[0] = add2(sub2(f[0], mulx2(om, sub2(f[0], e0), nz)), mulx2(bc2(__fmul_rn(P.gp, w0)), m3uF, nz));
+        f[0] = add2(sub2(f[0], mulx2(om, sub2(f[0], e0), nz)),
+                    mulx2(bc2(__fmul_rn(__fmul_rn(P.gp, w0), pow2f(SC))), m3uF, nz));
     }
 #pragma unroll
     for (int k = 1; k < Q; k += 2) {
         const float w = weight<Q>(k);
-        const float2 wr = mul2(bc2(w), rho);
+        const float2 wr = mul2(bc2(w * pow2f(SC)), rho);
         const float2 cu = dot_c2<Q>(k, u);
         const float cF = dot_c<Q>(k, P.fx, P.fy, P.fz);
         const float2 t = mul2(bc2(4.5f), cu);
@@ -480,8 +501,9 @@ __device__ __forceinline__ void collide_node_trt_dev2(float2 (&f)[Q], float2 drh
         const float2 sm = mulx2(bc2(0.5f), sub2(f[k], f[k + 1]), nz);
         const float2 a = mulx2(om, sub2(sp, ep), nz);
         const float2 b = mulx2(omm, sub2(sm, em), nz);
-        const float2 Sp = mulx2(bc2(__fmul_rn(P.gp, w)), fma2(mul2(bc2(9.0f), cu), bc2(cF), m3uF), nz);
-        const float2 Sm = bc2(__fmul_rn(__fmul_rn(P.gm, w), __fmul_rn(3.0f, cF)));
+        const float2 Sp =
+            mulx2(bc2(__fmul_rn(__fmul_rn(P.gp, w), pow2f(SC))), fma2(mul2(bc2(9.0f), cu), bc2(cF), m3uF), nz);
+        const float2 Sm = bc2(__fmul_rn(__fmul_rn(__fmul_rn(P.gm, w), pow2f(SC)), __fmul_rn(3.0f, cF)));
         const float2 nk = add2(sub2(sub2(f[k], a), b), add2(Sp, Sm));
         const float2 nr = add2(add2(sub2(f[k + 1], a), b), sub2(Sp, Sm));
         f[k] = nk;
@@ -509,9 +531,9 @@ __device__ __forceinline__ void update_pair_dev(float2 (&d)[Q], float2& rho, con
     }
     constexpr bool NEG = FORM == 0;
     float2 drho, ux, uy, uz;
-    node_moments_dev2<Q>(d, drho, rho, ux, uy, uz, bc2(cp.neg_zero));
-    if constexpr (ARITH == kArithTRT) collide_node_trt_dev2<Q>(d, drho, rho, ux, uy, uz, cp);
-    else collide_node_dev2<Q, NEG>(d, drho, rho, ux, uy, uz, cp);
+    node_moments_dev2<Q, kHalfShift>(d, drho, rho, ux, uy, uz, bc2(cp.neg_zero));
+    if constexpr (ARITH == kArithTRT) collide_node_trt_dev2<Q, kHalfShift>(d, drho, rho, ux, uy, uz, cp);
+    else collide_node_dev2<Q, NEG, kHalfShift>(d, drho, rho, ux, uy, uz, cp);
 }
 
 template <int Q, int ST>
@@ -519,7 +541,7 @@ __device__ __forceinline__ void moments_any(const typename Store<ST>::R (&f)[Q],
                                             typename Store<ST>::R& ux, typename Store<ST>::R& uy,
                                             typename Store<ST>::R& uz) {
     if constexpr (ST == 0) node_moments<Q>(f, rho, ux, uy, uz);
-    else if constexpr (ST == 1 || ST == 3) { float drho; node_moments_dev<Q>(f, drho, rho, ux, uy, uz); }
+    else if constexpr (ST == 1 || ST == 3) { float drho; node_moments_dev<Q, dev_shift<ST>()>(f, drho, rho, ux, uy, uz); }
     else node_moments_d<Q>(f, rho, ux, uy, uz);
 }
 
@@ -535,7 +557,9 @@ __device__ __forceinline__ typename Store<ST>::R wall_corrected(int k, typename 
         const double t = __dmul_rn(__dmul_rn(__dmul_rn(__dmul_rn(2.0, weight_d<Q>(k)), rho), cu), (double)cs2inv);
         return __dsub_rn(v, t);
     } else {
-        return __fsub_rn(v, wall_term<Q>(k, rho, dot_c_full<Q>(k, ub), cs2inv));
+        // FP16 storage: v is 2^12 times the deviation, so is the term (exact)
+        const float t = wall_term<Q>(k, rho, dot_c_full<Q>(k, ub), cs2inv);
+        return __fsub_rn(v, ST == 1 ? __fmul_rn(t, kHalfScale) : t);
     }
 }
 
@@ -684,11 +708,11 @@ __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, c
             f[k] = v;
         } else if (cx > 0) {
             float prev = __shfl_up_sync(kFull, v.y, 1);
-            if (edge_lo) prev = (active && xm >= 0) ? __half2float(__ldg(src + row + xm)) : 0.0f;
+            if (edge_lo) prev = (active && xm >= 0) ? Store<1>::ld(src, row + xm) : 0.0f;
             f[k] = make_float2(prev, v.x);
         } else {
             float next = __shfl_down_sync(kFull, v.x, 1);
-            if (edge_hi) next = (active && xp2 >= 0) ? __half2float(__ldg(src + row + xp2)) : 0.0f;
+            if (edge_hi) next = (active && xp2 >= 0) ? Store<1>::ld(src, row + xp2) : 0.0f;
             f[k] = make_float2(v.y, next);
         }
     }
@@ -697,8 +721,8 @@ __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, c
 #pragma unroll
         for (int k = 1; k < Q; ++k) {
             const long long slot = (long long)rev_of(k) * g.ks + node0;
-            if ((L0 >> rev_of(k)) & 1u) f[k].x = __half2float(__ldg(src + slot));
-            if ((L1 >> rev_of(k)) & 1u) f[k].y = __half2float(__ldg(src + slot + 1));
+            if ((L0 >> rev_of(k)) & 1u) f[k].x = Store<1>::ld(src, slot);
+            if ((L1 >> rev_of(k)) & 1u) f[k].y = Store<1>::ld(src, slot + 1);
         }
     }
     float2 rho;
@@ -779,7 +803,7 @@ nat_collide_raw_k(Geo g, CollideParams cp, NativeParams np, const typename Store
     for (int k = 0; k < Q; ++k) f[k] = Store<ST>::ld(src, k * g.ks + node);
     const R rho = (R)rho_f[node];
     const R ux = (R)u_f[node], uy = (R)u_f[g.ks + node], uz = (R)u_f[2 * g.ks + node];
-    collide_any<Q, ST, ARITH>(f, rho, ux, uy, uz, (ST == 1 || ST == 3) ? __fsub_rn((float)rho, 1.0f) : 0.0f, cp);
+    collide_any<Q, ST, ARITH>(f, rho, ux, uy, uz, raw_drho<ST>((float)rho), cp);
     store_node<Q, ST, MASK>(dst, g, np, types, L, nb, node, rho, f);
 }
 
@@ -817,7 +841,7 @@ nat_aa_even_k(Geo g, CollideParams cp, NativeParams np, typename Store<ST>::T* _
         // the first collision of a RAW state uses the rho/u fields
         rho = (R)rho_f[node];
         const R ux = (R)u_f[node], uy = (R)u_f[g.ks + node], uz = (R)u_f[2 * g.ks + node];
-        const float drho = (ST == 1 || ST == 3) ? __fsub_rn((float)rho, 1.0f) : 0.0f;
+        const float drho = raw_drho<ST>((float)rho);
         collide_any<Q, ST, ARITH>(f, rho, ux, uy, uz, drho, cp);
     } else {
         update_node<Q, ST, ARITH>(f, rho, cp);

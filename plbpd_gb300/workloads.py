@@ -4,6 +4,8 @@ sphere_mask: random spheres (radius uniform in [rmin, rmax]) dropped at
 uniform positions until the solid fraction reaches the target; periodic axes
 wrap, the others clip.  porous_mask: the same with small radii, to a target
 porosity (fluid fraction).  Both return uint8 arrays (nz, ny, nx), 1 = solid.
+taylor_green_state: the D3Q19 Taylor-Green start of the 256^3 periodic
+workload in plbpd's Field layout.
 """
 from __future__ import annotations
 
@@ -69,3 +71,40 @@ def batch_domains(count: int = 512, seed: int = 20261203, lmin: int = 16, lmax: 
         force = 8.0 * nu * 0.02 / (h * h)
         out.append((L, tau, por, force, seed + 1 + i))
     return out
+
+
+def taylor_green_state(n_side: int, out_n=None, out_rho=None, out_u=None, seed: int = 20261203):
+    """rho = 1 + 1e-3 N(0,1), u = Taylor-Green of amplitude 0.02 + 1e-4 N(0,1)
+    per component on a 2 pi / n grid, and n = EqlbDist(rho, u) with the
+    rounding of src/EqlbDist.hpp:26-38, on the interior of plbpd-layout D3Q19
+    arrays (n+2, n+2, n+2, V).  Returns (n, rho, u)."""
+    from . import capi
+    q = 19
+    rng = np.random.default_rng(seed)
+    N = n_side
+    shape3 = (N, N, N)
+    rho = (1.0 + 1e-3 * rng.standard_normal(shape3)).astype(np.float32)
+    ax = 2.0 * np.pi * np.arange(N) / N
+    zc, yc, xc = np.meshgrid(ax, ax, ax, indexing="ij")
+    A = 0.02
+    ux = (A * np.sin(xc) * np.cos(yc) * np.cos(zc) + 1e-4 * rng.standard_normal(shape3)).astype(np.float32)
+    uy = (-A * np.cos(xc) * np.sin(yc) * np.cos(zc) + 1e-4 * rng.standard_normal(shape3)).astype(np.float32)
+    uz = (1e-4 * rng.standard_normal(shape3)).astype(np.float32)
+    del zc, yc, xc
+    full = (N + 2, N + 2, N + 2)
+    n_arr = out_n if out_n is not None else np.zeros(full + (q,), np.float32)
+    r_arr = out_rho if out_rho is not None else np.zeros(full + (1,), np.float32)
+    u_arr = out_u if out_u is not None else np.zeros(full + (3,), np.float32)
+    r_arr[1:-1, 1:-1, 1:-1, 0] = rho
+    u_arr[1:-1, 1:-1, 1:-1, 0] = ux
+    u_arr[1:-1, 1:-1, 1:-1, 1] = uy
+    u_arr[1:-1, 1:-1, 1:-1, 2] = uz
+    c, w, _, _ = capi.model_tables("D3Q19")
+    usq = (ux * ux + uy * uy) + uz * uz
+    for k in range(q):
+        cu = (np.float32(c[k, 0]) * ux + np.float32(c[k, 1]) * uy) + np.float32(c[k, 2]) * uz
+        wr = (w[k] * rho).astype(np.float64)
+        cud = cu.astype(np.float64)
+        br = 1.0 + 3.0 * cud + 4.5 * cud * cud - 1.5 * usq.astype(np.float64)
+        n_arr[1:-1, 1:-1, 1:-1, k] = (wr * br).astype(np.float32)
+    return n_arr, r_arr, u_arr

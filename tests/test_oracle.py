@@ -141,3 +141,26 @@ def test_port_matches_live_reference(seed, variant, arith):
     p.step(15)
     for w in (po.N, po.NTMP, po.RHO, po.U):
         assert_bitexact(p.get(w), r.get(w), f"{cfg['model']} field {w}")
+
+
+def test_half_rounding_matches_ieee_binary16():
+    """orc_round_half is binary16 round-to-nearest-even (numpy's float16 is
+    the independent check); orc_store_half keeps d * 2^12 in it."""
+    lib = po.port_lib()
+    rng = np.random.default_rng(4)
+    mags = 10.0 ** rng.uniform(-12, 4.9, 4000)
+    vals = (mags * rng.choice([-1.0, 1.0], mags.size)).astype(np.float32)
+    edge = np.array([0.0, -0.0, 6.1035156e-05, 5.9604645e-08, 2.9802322e-08, 65504.0, 65520.0, 1e9,
+                     1.0 + 2.0 ** -11, 1.0 + 3 * 2.0 ** -11], np.float32)
+    for v in np.concatenate([vals, edge]):
+        want = np.float32(np.float16(v))
+        got = np.float32(lib.orc_round_half(float(v)))
+        assert got.tobytes() == want.tobytes() or (np.isinf(got) and np.isinf(want)), (v, got, want)
+        with np.errstate(over="ignore"):
+            want_s = np.float32(np.float32(np.float16(np.float32(v) * np.float32(4096.0))) / np.float32(4096.0))
+        got_s = np.float32(lib.orc_store_half(float(v)))
+        assert got_s.tobytes() == want_s.tobytes() or (np.isinf(got_s) and np.isinf(want_s)), (v, got_s, want_s)
+    # the scale keeps 11 bits where binary16 alone has subnormals
+    d = np.float32(3.0e-6)
+    assert abs(lib.orc_store_half(float(d)) - d) <= d * 2.0 ** -11
+    assert abs(np.float32(np.float16(d)) - d) > d * 2.0 ** -9
