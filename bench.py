@@ -238,13 +238,22 @@ def run_reference_arm(args):
 
 
 # ---------------------------------------------------------------------------
-def read_traffic():
-    """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
+# the fused-step kernel of each autotuner variant for FP32 storage (D3Q19, no mask)
+VARIANT_KERNEL = {0: "nat_fused_k<19,fp32,nomask> (one node a thread)",
+                  1: "nat_fused_h2_k<19,fp32,nomask,form 0> (two nodes a thread, paired FP32)",
+                  2: "nat_fused_h2_k<19,fp32,nomask,form 1> (two nodes a thread, paired FP32)",
+                  3: "nat_fused_h2_k<19,fp32,nomask,form 2> (two nodes a thread, scalar update)"}
+
+
+def read_traffic(variant: int):
+    """DRAM bytes per launch of the variant's kernel from the committed ncu
+    summary (lines `traffic_bytes_per_launch[variant N]: B`)."""
     path = os.path.join(ROOT, "profiles", "nat_fused_d3q19_256.md")
     if not os.path.exists(path):
         return None
+    key = f"traffic_bytes_per_launch[variant {variant}]:"
     for line in open(path):
-        if line.strip().startswith("traffic_bytes_per_launch:"):
+        if line.strip().startswith(key):
             try:
                 return float(line.split(":", 1)[1].strip())
             except ValueError:
@@ -337,13 +346,14 @@ def run_gpu_arm(args):
     h2d = (pin_n.nbytes + pin_rho.nbytes + pin_u.nbytes) / args.steps
     d2h = (out_rho.nbytes + out_u.nbytes) / args.steps
     mass = s.conservation()[0]
+    variant = s.variant()
     s.close()
 
     if rank != 0:
         return 0
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_CELL * cells / (kms * 1e-3) / 1e9
-    traffic = read_traffic()
+    traffic = read_traffic(variant)
     cs = clk.summary() or clk2.summary()
     line = {
         "metric": "MLUPS", "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
@@ -357,8 +367,8 @@ def run_gpu_arm(args):
                 "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "nat_fused_k<19,fp32,nomask>", "bytes_per_cell": BYTES_PER_CELL,
-                     "kernel_ms": round(kms, 4)},
+                     "kernel": VARIANT_KERNEL.get(variant, f"variant {variant}"), "variant": variant,
+                     "bytes_per_cell": BYTES_PER_CELL, "kernel_ms": round(kms, 4)},
         "gpu_launches": int(args.steps),
         "clocks": cs,
         "mass_after": mass,

@@ -97,8 +97,10 @@ int nat_fused_step(int q, int storage, int arith, bool has_mask, const Geo& g, c
 }
 
 int nat_fused_variants(int q, int storage, int arith, bool moving, const Geo& g) {
-    if (storage != 1 || g.nx % 2 != 0) return 1;
-    return nat_h2_variant_count(q, arith, moving);
+    if (g.nx % 2 != 0) return 1;
+    if (storage == 1) return nat_h2_variant_count(q, arith, moving);
+    if ((storage == 3 && arith != kArithTRT) || (storage == 0 && arith == kArithFP32)) return moving ? 1 : kPair32Variants;
+    return 1;
 }
 
 int nat_collide_raw(int q, int storage, int arith, bool has_mask, const Geo& g, const CollideParams& cp,

@@ -511,11 +511,70 @@ __device__ __forceinline__ void collide_node_trt_dev2(float2 (&f)[Q], float2 drh
     }
 }
 
-// update_node<Q, 1, ARITH> for two nodes.  FORM 0 and 1: paired, c.v of
-// collide_node_dev2 with NEG = 1 and 0; FORM 2: the scalar update of each
-// node (one instruction stream a node, more instructions, other registers).
-template <int Q, int ARITH, int FORM>
+// update_node<Q, ST, ARITH> of deviation storage (ST 1 or 3, scale SC) for
+// two nodes.  NEG as in collide_node_dev2.
+template <int Q, int ARITH, bool NEG, int SC>
 __device__ __forceinline__ void update_pair_dev(float2 (&d)[Q], float2& rho, const CollideParams& cp) {
+    float2 drho, ux, uy, uz;
+    node_moments_dev2<Q, SC>(d, drho, rho, ux, uy, uz, bc2(cp.neg_zero));
+    if constexpr (ARITH == kArithTRT) collide_node_trt_dev2<Q, SC>(d, drho, rho, ux, uy, uz, cp);
+    else collide_node_dev2<Q, NEG, SC>(d, drho, rho, ux, uy, uz, cp);
+}
+
+// node_moments + collide_node<Q, kArithFP32> (plbpd's FP32 body sequence
+// for every direction) for two nodes, op for op.
+template <int Q, bool NEG>
+__device__ __forceinline__ void update_pair_fp32(float2 (&f)[Q], float2& rho, const CollideParams& P) {
+    const float2 nz = bc2(P.neg_zero);
+    float2 r = bc2(0.0f), jx = bc2(0.0f), jy = bc2(0.0f), jz = bc2(0.0f);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        r = add2(r, f[k]);
+        if (Lattice<Q>::cx(k) > 0) jx = add2(jx, f[k]);
+        if (Lattice<Q>::cx(k) < 0) jx = sub2(jx, f[k]);
+        if (Lattice<Q>::cy(k) > 0) jy = add2(jy, f[k]);
+        if (Lattice<Q>::cy(k) < 0) jy = sub2(jy, f[k]);
+        if (Lattice<Q>::cz(k) > 0) jz = add2(jz, f[k]);
+        if (Lattice<Q>::cz(k) < 0) jz = sub2(jz, f[k]);
+    }
+    const float2 rinv = div2(1.0f, r);
+    rho = r;
+    const float2 tr = div2(P.tau, rho);
+    Vel2 u;
+    float2 (&v)[3] = u.v;
+    v[0] = add2(mulx2(jx, rinv, nz), mulx2(bc2(P.fx), tr, nz));
+    v[1] = add2(mulx2(jy, rinv, nz), mulx2(bc2(P.fy), tr, nz));
+    v[2] = add2(mulx2(jz, rinv, nz), mulx2(bc2(P.fz), tr, nz));
+    if (!NEG) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) u.nv[a] = mul2(bc2(-1.0f), v[a]);
+    }
+    const float2 usq = add2(add2(mulx2(v[0], v[0], nz), mulx2(v[1], v[1], nz)), mulx2(v[2], v[2], nz));
+    const float2 kusq = mulx2(bc2(-1.5f), usq, nz);
+    const float2 om = bc2(P.omega), omc = bc2(P.omc);
+    // a zero's sign in c.v cannot reach the result: cu^2 is +0 and 3 cu + 1 is 1
+    float2 cu_prev = bc2(0.0f);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        const float2 cu = (k == 0) ? bc2(0.0f)
+                          : !NEG   ? dot_c2<Q>(k, u)
+                          : (k & 1) ? dot_c2_fwd<Q>(k, v)
+                                    : mul2(bc2(-1.0f), cu_prev);
+        cu_prev = cu;
+        const float2 cusq = mul2(cu, cu);
+        float2 neq = fma2(bc2(3.0f), cu, bc2(1.0f));
+        neq = fma2(bc2(4.5f), cusq, neq);
+        neq = add2(neq, kusq);
+        neq = mul2(neq, rho);
+        neq = mul2(neq, bc2(weight<Q>(k)));
+        f[k] = fma2(omc, f[k], mul2(om, neq));
+    }
+}
+
+// The update of a pair kernel: FORM 0 and 1 paired (NEG = FORM == 0),
+// FORM 2 the scalar update of each node (other registers and schedule).
+template <int Q, int ST, int ARITH, int FORM>
+__device__ __forceinline__ void update_pair(float2 (&d)[Q], float2& rho, const CollideParams& cp) {
     if constexpr (FORM == 2) {
         float a[Q], b[Q];
 #pragma unroll
@@ -523,17 +582,16 @@ __device__ __forceinline__ void update_pair_dev(float2 (&d)[Q], float2& rho, con
             a[k] = d[k].x;
             b[k] = d[k].y;
         }
-        update_node<Q, 1, ARITH>(a, rho.x, cp);
-        update_node<Q, 1, ARITH>(b, rho.y, cp);
+        update_node<Q, ST, ARITH>(a, rho.x, cp);
+        update_node<Q, ST, ARITH>(b, rho.y, cp);
 #pragma unroll
         for (int k = 0; k < Q; ++k) d[k] = make_float2(a[k], b[k]);
-        return;
+    } else if constexpr (ST == 0) {
+        static_assert(ARITH == kArithFP32, "paired FP32 storage runs plbpd's FP32 body arithmetic only");
+        update_pair_fp32<Q, FORM == 0>(d, rho, cp);
+    } else {
+        update_pair_dev<Q, ARITH, FORM == 0, dev_shift<ST>()>(d, rho, cp);
     }
-    constexpr bool NEG = FORM == 0;
-    float2 drho, ux, uy, uz;
-    node_moments_dev2<Q, kHalfShift>(d, drho, rho, ux, uy, uz, bc2(cp.neg_zero));
-    if constexpr (ARITH == kArithTRT) collide_node_trt_dev2<Q, kHalfShift>(d, drho, rho, ux, uy, uz, cp);
-    else collide_node_dev2<Q, NEG, kHalfShift>(d, drho, rho, ux, uy, uz, cp);
 }
 
 template <int Q, int ST>
@@ -667,11 +725,15 @@ nat_fused_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::
 // it together (the shuffles), lanes past the end of their row with
 // active = false.  A lane's neighbour lane holds the neighbouring pair of the
 // same row unless x0 is 0 or x0 + 2 is nx, which the edge loads cover.
-template <int Q, bool MASK, bool MOVING, int ARITH, int FORM = 0>
+//
+// The same two-node scheme serves FP32 and FP32-deviation storage (ST 0 and
+// 3: one aligned float2 a lane and direction), where it halves the
+// instructions a node takes and doubles the bytes a thread has in flight.
+template <int Q, bool MASK, bool MOVING, int ARITH, int FORM = 0, int ST = 1>
 __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, const NativeParams& np,
-                                        const __half* __restrict__ src, __half* __restrict__ dst,
-                                        const uint8_t* __restrict__ types, int lane, int x0, int y, int z,
-                                        bool active) {
+                                        const typename Store<ST>::T* __restrict__ src,
+                                        typename Store<ST>::T* __restrict__ dst, const uint8_t* __restrict__ types,
+                                        int lane, int x0, int y, int z, bool active) {
     const unsigned kFull = 0xffffffffu;
     const int ym = y == 0 ? (g.wrap_y ? g.ny - 1 : y) : y - 1;
     const int yp = y == g.ny - 1 ? (g.wrap_y ? 0 : y) : y + 1;
@@ -703,16 +765,19 @@ __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, c
         const int cx = Lattice<Q>::cx(k), cy = Lattice<Q>::cy(k), cz = Lattice<Q>::cz(k);
         const long long row = (long long)k * g.ks + zo[1 - cz] + yo[1 - cy];
         float2 v = make_float2(0.0f, 0.0f);
-        if (active) v = __half22float2(__ldg(reinterpret_cast<const __half2*>(src + row + x0)));
+        if (active) {
+            if constexpr (ST == 1) v = __half22float2(__ldg(reinterpret_cast<const __half2*>(src + row + x0)));
+            else v = __ldg(reinterpret_cast<const float2*>(src + row + x0));
+        }
         if (cx == 0) {
             f[k] = v;
         } else if (cx > 0) {
             float prev = __shfl_up_sync(kFull, v.y, 1);
-            if (edge_lo) prev = (active && xm >= 0) ? Store<1>::ld(src, row + xm) : 0.0f;
+            if (edge_lo) prev = (active && xm >= 0) ? Store<ST>::ld(src, row + xm) : 0.0f;
             f[k] = make_float2(prev, v.x);
         } else {
             float next = __shfl_down_sync(kFull, v.x, 1);
-            if (edge_hi) next = (active && xp2 >= 0) ? Store<1>::ld(src, row + xp2) : 0.0f;
+            if (edge_hi) next = (active && xp2 >= 0) ? Store<ST>::ld(src, row + xp2) : 0.0f;
             f[k] = make_float2(v.y, next);
         }
     }
@@ -721,29 +786,33 @@ __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, c
 #pragma unroll
         for (int k = 1; k < Q; ++k) {
             const long long slot = (long long)rev_of(k) * g.ks + node0;
-            if ((L0 >> rev_of(k)) & 1u) f[k].x = Store<1>::ld(src, slot);
-            if ((L1 >> rev_of(k)) & 1u) f[k].y = Store<1>::ld(src, slot + 1);
+            if ((L0 >> rev_of(k)) & 1u) f[k].x = Store<ST>::ld(src, slot);
+            if ((L1 >> rev_of(k)) & 1u) f[k].y = Store<ST>::ld(src, slot + 1);
         }
     }
     float2 rho;
-    update_pair_dev<Q, ARITH, FORM>(f, rho, cp);
+    update_pair<Q, ST, ARITH, FORM>(f, rho, cp);
     if (MASK && MOVING && (L0 | L1)) {
         const Nbr n0(g, x0, y, z), n1(g, x0 + 1, y, z);
 #pragma unroll
         for (int k = 1; k < Q; ++k) {
             if ((L0 >> k) & 1u)
-                f[k].x = wall_corrected<Q, 1>(k, f[k].x, rho.x, np.vel[__ldg(types + n0.at<Q>(k, +1)) & kVelMask],
-                                              np.cs2inv);
+                f[k].x = wall_corrected<Q, ST>(k, f[k].x, rho.x, np.vel[__ldg(types + n0.at<Q>(k, +1)) & kVelMask],
+                                               np.cs2inv);
             if ((L1 >> k) & 1u)
-                f[k].y = wall_corrected<Q, 1>(k, f[k].y, rho.y, np.vel[__ldg(types + n1.at<Q>(k, +1)) & kVelMask],
-                                              np.cs2inv);
+                f[k].y = wall_corrected<Q, ST>(k, f[k].y, rho.y, np.vel[__ldg(types + n1.at<Q>(k, +1)) & kVelMask],
+                                               np.cs2inv);
         }
     }
 #pragma unroll
     for (int k = 0; k < Q; ++k) {
-        const __half2 v = __float22half2_rn(f[k]);
-        __stcs(reinterpret_cast<unsigned int*>(dst + (long long)k * g.ks + node0),
-               *reinterpret_cast<const unsigned int*>(&v));
+        if constexpr (ST == 1) {
+            const __half2 v = __float22half2_rn(f[k]);
+            __stcs(reinterpret_cast<unsigned int*>(dst + (long long)k * g.ks + node0),
+                   *reinterpret_cast<const unsigned int*>(&v));
+        } else {
+            __stcs(reinterpret_cast<float2*>(dst + (long long)k * g.ks + node0), f[k]);
+        }
     }
 }
 
@@ -761,23 +830,25 @@ struct H2Variant {
 constexpr int kH2Variants = kFusedVariants;
 constexpr H2Variant kH2Variant[kH2Variants] = {{0, 0}, {1, 0}, {2, 0}, {0, 72}, {1, 72}, {0, 80}, {1, 80}};
 
-template <int Q, bool MASK, bool MOVING, int ARITH, int BX, int FORM>
+template <int Q, bool MASK, bool MOVING, int ARITH, int BX, int FORM, int ST = 1>
 __global__ void __launch_bounds__(BX)
-nat_fused_h2_k(Geo g, CollideParams cp, NativeParams np, const __half* __restrict__ src, __half* __restrict__ dst,
-               const uint8_t* __restrict__ types) {
+nat_fused_h2_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::T* __restrict__ src,
+               typename Store<ST>::T* __restrict__ dst, const uint8_t* __restrict__ types) {
     const int lane = threadIdx.x & 31;   // a warp is 32 consecutive pairs of one row
     const int x0 = 2 * (blockIdx.x * BX + threadIdx.x);
-    h2_pair<Q, MASK, MOVING, ARITH, FORM>(g, cp, np, src, dst, types, lane, x0, blockIdx.y, blockIdx.z, x0 < g.nx);
+    h2_pair<Q, MASK, MOVING, ARITH, FORM, ST>(g, cp, np, src, dst, types, lane, x0, blockIdx.y, blockIdx.z,
+                                              x0 < g.nx);
 }
 
 // The same kernel with at most NR registers a thread.
-template <int Q, bool MASK, bool MOVING, int ARITH, int BX, int FORM, int NR>
+template <int Q, bool MASK, bool MOVING, int ARITH, int BX, int FORM, int NR, int ST = 1>
 __global__ void __maxnreg__(NR)
-nat_fused_h2_kr(Geo g, CollideParams cp, NativeParams np, const __half* __restrict__ src, __half* __restrict__ dst,
-                const uint8_t* __restrict__ types) {
+nat_fused_h2_kr(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::T* __restrict__ src,
+                typename Store<ST>::T* __restrict__ dst, const uint8_t* __restrict__ types) {
     const int lane = threadIdx.x & 31;
     const int x0 = 2 * (blockIdx.x * BX + threadIdx.x);
-    h2_pair<Q, MASK, MOVING, ARITH, FORM>(g, cp, np, src, dst, types, lane, x0, blockIdx.y, blockIdx.z, x0 < g.nx);
+    h2_pair<Q, MASK, MOVING, ARITH, FORM, ST>(g, cp, np, src, dst, types, lane, x0, blockIdx.y, blockIdx.z,
+                                              x0 < g.nx);
 }
 
 // First collision from a RAW state: n at the node itself and the rho/u fields.
@@ -1166,6 +1237,31 @@ int launch_fused_h2(const Geo& g, const CollideParams& cp, const NativeParams& n
     return (int)cudaGetLastError();
 }
 
+// FP32 and FP32-deviation storage (BGK, FP32 arithmetic) with even nx: the
+// single-node kernel is variant 0, the pair kernel in forms 0, 1 and 2 are
+// variants 1-3.  Moving walls and other arithmetics have the single-node
+// kernel only.
+constexpr int kPair32Variants = 4;
+
+template <int Q, int ST, bool MASK>
+int launch_fused_pair32(const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
+                        const uint8_t* types, int variant, cudaStream_t st) {
+    static_assert(ST == 0 || ST == 3, "FP32 storages only");
+    using T = typename Store<ST>::T;
+    auto s2 = (const T*)src;
+    auto d2 = (T*)dst;
+    auto go = [&](auto bxc) {
+        constexpr int BX = decltype(bxc)::value;
+        const dim3 grid = seg_grid(g, BX, 2);
+        if (variant == 2) nat_fused_h2_k<Q, MASK, false, kArithFP32, BX, 1, ST><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types);
+        else if (variant == 3) nat_fused_h2_k<Q, MASK, false, kArithFP32, BX, 2, ST><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types);
+        else nat_fused_h2_k<Q, MASK, false, kArithFP32, BX, 0, ST><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types);
+    };
+    if (block_x(g, 2) == kBlockX) go(std::integral_constant<int, kBlockX>{});
+    else go(std::integral_constant<int, 32>{});
+    return (int)cudaGetLastError();
+}
+
 // One fused step (FP16 storage with even nx: the pair kernel).
 template <bool TRT, int Q>
 int fused_q(int storage, int arith, bool m, const Geo& g, const CollideParams& cp, const NativeParams& np,
@@ -1182,6 +1278,13 @@ int fused_q(int storage, int arith, bool m, const Geo& g, const CollideParams& c
                     if constexpr (Q == 19) return nat_fused_h2_bgk19(m, g, cp, np, src, dst, types, variant, st);
                     if constexpr (Q == 27) return nat_fused_h2_bgk27(m, g, cp, np, src, dst, types, variant, st);
                 }
+            }
+        }
+        if constexpr (!TRT && (ST == 3 || (ST == 0 && AR == kArithFP32))) {
+            if (variant > 0 && g.nx % 2 == 0 && !(m && np.moving)) {
+                if constexpr (Q == 9) return nat_fused_pair32_q9(ST, m, g, cp, np, src, dst, types, variant, st);
+                if constexpr (Q == 19) return nat_fused_pair32_q19(ST, m, g, cp, np, src, dst, types, variant, st);
+                if constexpr (Q == 27) return nat_fused_pair32_q27(ST, m, g, cp, np, src, dst, types, variant, st);
             }
         }
         return m ? launch_fused<Q, ST, true, AR>(g, cp, np, src, dst, types, st)

@@ -1,5 +1,7 @@
-"""The fused-step autotuner: every compiled variant of the FP16 pair kernel
-gives the oracle's bits, and a tuned solve runs one of them and records it."""
+"""The fused-step autotuner: every compiled variant of the fused step (the
+FP16 pair kernel's forms; for FP32 and FP32_DEV storage the single-node and
+the pair kernel) gives the oracle's bits, and a tuned solve runs one of them
+and records it."""
 import numpy as np
 import pytest
 
@@ -12,10 +14,15 @@ pytestmark = pytest.mark.gpu
 PAIR_CASES = ["torus_d3q19", "obstacles_d3q19", "channel_d2q9", "obstacles_torus_d3q27", "duct_d3q27"]
 
 
-def oracle_after(case, steps):
+STORAGE = {"fp16": ("STORAGE_FP16_DEV", "ARITH_FP32", po.ARITH_FP16DEV),
+           "fp32": ("STORAGE_FP32", "ARITH_FP32", po.ARITH_FP32),
+           "fp32dev": ("STORAGE_FP32_DEV", "ARITH_FP32", po.ARITH_FP32DEV)}
+
+
+def oracle_after(case, steps, storage="fp16"):
     cfg = NATIVE_CASES[case]
     mask = mask_for(case, cfg)
-    p = po.Port(**cfg, mode=po.MODE_NATIVE, mask=mask, arith=po.ARITH_FP16DEV)
+    p = po.Port(**cfg, mode=po.MODE_NATIVE, mask=mask, arith=STORAGE[storage][2])
     p._cfg = cfg
     p.initialize()
     start = perturbed_start(p, 11)
@@ -24,8 +31,9 @@ def oracle_after(case, steps):
     return cfg, mask, start, p
 
 
-def gpu_solve(capi, cfg, mask, start, steps):
-    s = capi.Solve.create(**cfg, semantics=capi.SEMANTICS_NATIVE, storage=capi.STORAGE_FP16_DEV)
+def gpu_solve(capi, cfg, mask, start, steps, storage="fp16"):
+    st, ar, _ = STORAGE[storage]
+    s = capi.Solve.create(**cfg, semantics=capi.SEMANTICS_NATIVE, storage=getattr(capi, st), arith=getattr(capi, ar))
     if mask is not None:
         s.set_mask(mask)
     s.initialize()
@@ -34,16 +42,19 @@ def gpu_solve(capi, cfg, mask, start, steps):
     return s
 
 
+@pytest.mark.parametrize("storage", sorted(STORAGE))
 @pytest.mark.parametrize("case", PAIR_CASES)
-def test_every_variant_matches_oracle(case):
+def test_every_variant_matches_oracle(case, storage):
+    """FP16: the pair kernel's seven compiled forms; FP32 and FP32_DEV: the
+    single-node kernel and the pair kernel's three forms."""
     from plbpd_gb300 import capi
-    cfg, mask, start, p = oracle_after(case, 20)
+    cfg, mask, start, p = oracle_after(case, 20, storage)
     try:
         for v in range(capi.tune_variants()):
             capi.tune_force(v)
-            with gpu_solve(capi, cfg, mask, start, 20) as s:
+            with gpu_solve(capi, cfg, mask, start, 20, storage) as s:
                 assert s.variant() in (v, 0)
-                compare(s, p, mask, f"{case} variant {v}")
+                compare(s, p, mask, f"{case} {storage} variant {v}")
     finally:
         capi.tune_force(-1)
 
