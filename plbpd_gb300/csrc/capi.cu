@@ -652,6 +652,26 @@ int sync(plb_solve* s) {
 
 int plb::check_params(const plb_params* p) { return validate(p); }
 
+namespace {
+// Waits for `st`'s work, then replaces it with a stream of CUDA priority
+// `priority`.  Captured graphs are not bound to a stream, and memory the old
+// stream allocated is usable once its work is done.
+int restream(cudaStream_t* st, int priority) {
+    cudaStream_t ns = nullptr;
+    PLB_CUDA(cudaStreamSynchronize(*st));
+    PLB_CUDA(cudaStreamCreateWithPriority(&ns, cudaStreamNonBlocking, priority));
+    cudaStreamDestroy(*st);
+    *st = ns;
+    return PLB_OK;
+}
+}  // namespace
+
+int plb::set_solve_priority(plb_solve* s, int priority) {
+    if (!s) return fail(PLB_EINVAL, "solve is null");
+    PLB_CUDA(cudaSetDevice(s->p.device));
+    return restream(&s->stream, priority);
+}
+
 // ===========================================================================
 extern "C" {
 
@@ -1101,12 +1121,12 @@ struct plb_batch {
     int q = 0, storage = 0, arith = 0, device = 0;
     cudaStream_t stream = nullptr;
     BatchDomain* d_doms = nullptr;
-    int4* d_tiles = nullptr;   // warp tasks (domain, z, first node of the plane, 0)
+    int4* d_tiles = nullptr;   // warp tasks (domain, z, first node of the plane, 1 for a pair task)
     int ntiles = 0;
     int blocks = 0;
     int64_t cells = 0;
     bool moving = false;   // some member has a moving wall
-    bool pairs = false;    // FP16 with every nx even: the pair kernel, 64-node tasks
+    bool pairs = false;    // some domain has even nx: 64-node pair tasks beside 32-node ones
     int graph_steps = 64;
     cudaGraphExec_t graph = nullptr;
     std::vector<BatchDomain> h_doms;
@@ -1188,6 +1208,12 @@ int batch_capture(plb_batch* b) {
 
 }  // namespace
 
+int plb::set_batch_priority(plb_batch* b, int priority) {
+    if (!b) return fail(PLB_EINVAL, "batch is null");
+    PLB_CUDA(cudaSetDevice(b->device));
+    return restream(&b->stream, priority);
+}
+
 extern "C" {
 
 int plb_batch_create(int32_t n, plb_solve* const* solves, plb_batch** out) {
@@ -1216,15 +1242,16 @@ int plb_batch_create(int32_t n, plb_solve* const* solves, plb_batch** out) {
         batch_release(b);
         return fail(PLB_ECUDA, "cudaStreamCreate");
     }
-    b->pairs = b->storage == PLB_STORAGE_FP16_DEV;
-    for (int i = 0; i < n; ++i) b->pairs = b->pairs && solves[i]->g.nx % 2 == 0;
-    const int per_task = b->pairs ? 64 : 32;
+    // a domain with even nx runs as pair tasks (two nodes a lane, 64 a warp)
     std::vector<int4> tiles;
     for (int i = 0; i < n; ++i) {
         const Geo& g = solves[i]->g;
+        const bool pair = g.nx % 2 == 0;
+        const int per_task = pair ? 64 : 32;
+        b->pairs |= pair;
         const int plane = g.nx * g.ny;   // nodes of one z plane, x fastest
         for (int z = 0; z < g.nz; ++z)
-            for (int i0 = 0; i0 < plane; i0 += per_task) tiles.push_back(make_int4(i, z, i0, 0));
+            for (int i0 = 0; i0 < plane; i0 += per_task) tiles.push_back(make_int4(i, z, i0, pair ? 1 : 0));
         b->cells += g.cells();
     }
     b->ntiles = (int)tiles.size();

@@ -8,6 +8,8 @@
 #include "lattice.cuh"
 
 struct plb_params;
+struct plb_solve;
+struct plb_batch;
 
 namespace plb {
 
@@ -17,6 +19,11 @@ void record_error(const std::string& msg);
 // plb_solve_create's checks of a parameter block: PLB_OK, or an error code
 // with the message recorded.
 int check_params(const plb_params* p);
+
+// Moves a solve's / a batch's work onto a new stream of CUDA priority
+// `priority` (after the old stream's work); the solve server ranks its lanes.
+int set_solve_priority(plb_solve* s, int priority);
+int set_batch_priority(plb_batch* b, int priority);
 
 // Boundary description handed to the REFERENCE-semantics kernels.  Faces are
 // numbered east, west, north, south, up, down (plbpd's src/Boundary.cpp:17-18).

@@ -1078,7 +1078,14 @@ nat_gather_k(Geo g, NativeParams np, const typename Store<ST>::T* __restrict__ s
 // nat_fused_k: the same gather, arithmetic and bounce-back, so a domain's
 // result does not depend on which other domains share its batch.  Descriptor
 // fields are read where they are used (every lane reads the same address).
-template <int Q, int ST, int ARITH, bool MOVING>
+//
+// PAIRS: the batch also holds tasks of 64 consecutive nodes (task .w = 1,
+// domains with even nx), which run the two-node pair kernel's work: a pair
+// never straddles a row (nx is even), and the rows of a warp's pairs differ,
+// so each lane forms its own row offsets.  A task's kind is the same for the
+// whole warp.  FP16 pairs use the paired update (form 0), FP32 storages the
+// scalar update of each node (form 2), which serves every arithmetic.
+template <int Q, int ST, int ARITH, bool MOVING, bool PAIRS = false>
 __global__ void __launch_bounds__(kBatchTile)
 nat_batch_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks, int ntasks, int parity) {
     using T = typename Store<ST>::T;
@@ -1089,6 +1096,16 @@ nat_batch_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks
         const int4 tk = __ldg(tasks + t);
         const BatchDomain& D = doms[tk.x];
         const Geo g = D.g;
+        if (PAIRS && tk.w) {
+            const int i = tk.z + 2 * lane;
+            const bool active = i < g.nx * g.ny;
+            const int y = active ? (int)((unsigned)i / (unsigned)g.nx) : 0;
+            const int x0 = active ? i - y * g.nx : 0;
+            h2_pair<Q, true, MOVING, ARITH, ST == 1 ? 0 : 2, ST>(g, D.cp, D.np, static_cast<const T*>(D.f[parity]),
+                                                                static_cast<T*>(D.f[parity ^ 1]), D.types, lane, x0,
+                                                                y, tk.y, active);
+            continue;
+        }
         // 32 consecutive nodes of the plane z (flattened y * nx + x), so short
         // rows do not leave lanes idle
         const int i = tk.z + lane;
@@ -1108,28 +1125,6 @@ nat_batch_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks
         R rho;
         update_node<Q, ST, ARITH>(f, rho, D.cp);
         store_node<Q, ST, true, MOVING>(dst, g, np, types, L, nb, node, rho, f);
-    }
-}
-
-// FP16 batches of domains with even nx: the pair kernel's work over warp
-// tasks of 64 consecutive nodes (32 pairs) of one z plane.  A pair never
-// straddles a row (nx is even), and the rows of a warp's pairs differ, so
-// each lane forms its own row offsets.
-template <int Q, int ARITH, bool MOVING>
-__global__ void __launch_bounds__(kBatchTile)
-nat_batch_h2_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks, int ntasks, int parity) {
-    const int lane = threadIdx.x & 31;
-    const int warps = gridDim.x * (kBatchTile / 32);
-    for (int t = blockIdx.x * (kBatchTile / 32) + (threadIdx.x >> 5); t < ntasks; t += warps) {
-        const int4 tk = __ldg(tasks + t);
-        const BatchDomain& D = doms[tk.x];
-        const Geo g = D.g;
-        const int i = tk.z + 2 * lane;
-        const bool active = i < g.nx * g.ny;
-        const int y = active ? (int)((unsigned)i / (unsigned)g.nx) : 0;
-        const int x0 = active ? i - y * g.nx : 0;
-        h2_pair<Q, true, MOVING, ARITH>(g, D.cp, D.np, static_cast<const __half*>(D.f[parity]),
-                                        static_cast<__half*>(D.f[parity ^ 1]), D.types, lane, x0, y, tk.y, active);
     }
 }
 
@@ -1336,25 +1331,22 @@ int aa_q(int kind, int storage, int arith, bool m, const Geo& g, const CollidePa
     });
 }
 
-// Batches hold FP32, FP32-deviation or FP16 storage; `pairs`: FP16 batches
-// whose domains all have even nx run the pair kernel over 64-node tasks.
+// Batches hold FP32, FP32-deviation or FP16 storage; `pairs`: the task list
+// holds 64-node pair tasks (domains with even nx) beside 32-node ones.
 template <bool TRT, bool MV>
 const void* batch_kernel_for(int q, int storage, int arith, bool pairs) {
     if (storage == 2) return nullptr;
     const void* k = nullptr;
     with_storage_arith<TRT>(storage, arith, [&](auto stc, auto arc) {
         constexpr int ST = decltype(stc)::value == 2 ? 0 : decltype(stc)::value, AR = decltype(arc)::value;
-        if constexpr (ST == 1) {
-            if (pairs) {
-                k = q == 9 ? (const void*)nat_batch_h2_k<9, AR, MV>
-                  : q == 19 ? (const void*)nat_batch_h2_k<19, AR, MV>
-                  : q == 27 ? (const void*)nat_batch_h2_k<27, AR, MV> : nullptr;
-                return 0;
-            }
-        }
-        k = q == 9 ? (const void*)nat_batch_k<9, ST, AR, MV>
-          : q == 19 ? (const void*)nat_batch_k<19, ST, AR, MV>
-          : q == 27 ? (const void*)nat_batch_k<27, ST, AR, MV> : nullptr;
+        if (pairs)
+            k = q == 9 ? (const void*)nat_batch_k<9, ST, AR, MV, true>
+              : q == 19 ? (const void*)nat_batch_k<19, ST, AR, MV, true>
+              : q == 27 ? (const void*)nat_batch_k<27, ST, AR, MV, true> : nullptr;
+        else
+            k = q == 9 ? (const void*)nat_batch_k<9, ST, AR, MV>
+              : q == 19 ? (const void*)nat_batch_k<19, ST, AR, MV>
+              : q == 27 ? (const void*)nat_batch_k<27, ST, AR, MV> : nullptr;
         return 0;
     });
     return k;
@@ -1381,14 +1373,12 @@ int batch_step(int q, int storage, int arith, bool moving, bool pairs, const Bat
         constexpr int ST = decltype(stc)::value == 2 ? 0 : decltype(stc)::value, AR = decltype(arc)::value;
         auto go = [&](auto qc) {
             constexpr int Q = decltype(qc)::value;
-            if constexpr (ST == 1) {
-                if (pairs) {
-                    if (moving)
-                        nat_batch_h2_k<Q, AR, true><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);
-                    else
-                        nat_batch_h2_k<Q, AR, false><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);
-                    return (int)cudaGetLastError();
-                }
+            if (pairs) {
+                if (moving)
+                    nat_batch_k<Q, ST, AR, true, true><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);
+                else
+                    nat_batch_k<Q, ST, AR, false, true><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);
+                return (int)cudaGetLastError();
             }
             if (moving) nat_batch_k<Q, ST, AR, true><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);
             else nat_batch_k<Q, ST, AR, false><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);

@@ -6,9 +6,13 @@
 // (same lattice, storage and arithmetic) and advances them as one plb_batch;
 // a solo lane holds one large solve and advances it with the solve's own
 // kernels.  Each loop the scheduler
-//   1. admits queued requests in arrival order while their device bytes fit
-//      the budget (a request larger than the whole budget fails) and routes
-//      each to a new solo lane or to its class's batch lane,
+//   1. admits queued requests while their device bytes fit the budget (a
+//      request larger than the whole budget fails), the one with the fewest
+//      cell updates first unless the oldest has waited PLB_SERVER_MAX_WAIT
+//      seconds (default 30; PLB_SERVER_ORDER=fifo: arrival order), while the
+//      running requests hold fewer than PLB_SERVER_ACTIVE_CELLS cells
+//      (default 2^23), and routes each to a new solo lane or to its class's
+//      batch lane,
 //   2. collects the lanes whose tick has ended (an event per lane, polled):
 //      solves that have run all their steps retire -- rho and u are copied to
 //      host memory, the solve is destroyed, its bytes return to the budget,
@@ -19,6 +23,7 @@
 // stream-ordered, so retiring a solve does not synchronize the device.
 // Clients submit from any thread and wait on a condition variable.
 #include <atomic>
+#include <cmath>
 #include <chrono>
 #include <condition_variable>
 #include <cstdlib>
@@ -40,6 +45,8 @@
 namespace plb {
 void record_error(const std::string& msg);   // capi.cu: the plb_last_error() slot
 int check_params(const plb_params* p);       // capi.cu: plb_solve_create's validation
+int set_solve_priority(plb_solve* s, int priority);   // capi.cu: move onto a stream of that priority
+int set_batch_priority(plb_batch* b, int priority);
 }
 
 namespace {
@@ -77,6 +84,46 @@ using ClassKey = std::tuple<int, int, int, int>;   // q, storage, arith, collisi
 long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
 
 // Solves of at least this many cells run in their own lane.
+// Admission order.  Under overload the budget fills with admitted requests
+// that share the device, and a request's latency is its wait for admission
+// plus its share of the device; taking the smallest work first (with an age
+// bound so large requests are not starved) shortens the median wait without
+// changing the total work or its rate.
+bool fifo_order() {
+    static const bool v = [] {
+        const char* e = std::getenv("PLB_SERVER_ORDER");
+        return e && std::strcmp(e, "fifo") == 0;
+    }();
+    return v;
+}
+
+double max_wait_s() {
+    static const double v = [] {
+        const char* e = std::getenv("PLB_SERVER_MAX_WAIT");
+        const double x = e ? std::atof(e) : 0.0;
+        return x > 0.0 ? x : 30.0;
+    }();
+    return v;
+}
+
+double work_of(const Req* r) { return (double)r->p.nx * r->p.ny * r->p.nz * (double)r->steps; }
+
+int64_t cells_of(const Req* r) { return (int64_t)r->p.nx * r->p.ny * r->p.nz; }
+
+// Cells the running requests may hold together (PLB_SERVER_ACTIVE_CELLS).
+// Enough to keep the device saturated; more only makes the admitted
+// requests share it longer (every one finishes later) and costs the
+// scheduler thread more lanes to service.  A request larger than the cap
+// runs once nothing else is running.
+int64_t active_cells_cap() {
+    static const int64_t v = [] {
+        const char* e = std::getenv("PLB_SERVER_ACTIVE_CELLS");
+        const long long x = e ? std::atoll(e) : 0;
+        return (int64_t)(x > 0 ? x : (1LL << 23));
+    }();
+    return v;
+}
+
 long long solo_cells() {
     static const long long v = [] {
         const char* e = std::getenv("PLB_SERVER_SOLO_CELLS");
@@ -91,6 +138,7 @@ long long solo_cells() {
 struct plb_server {
     int device = 0;
     int64_t budget = 0, used = 0, peak = 0;
+    int64_t active_cells = 0;   // cells of the running requests (scheduler's admission cap)
     int tick = 100;
     Clock::time_point t0;
     std::thread th;
@@ -103,6 +151,7 @@ struct plb_server {
     // scheduler thread only
     std::map<ClassKey, std::unique_ptr<Lane>> batch_lanes;
     std::vector<std::unique_ptr<Lane>> solo_lanes;
+    int prio_least = 0, prio_greatest = 0;   // cudaDeviceGetStreamPriorityRange
 
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 };
@@ -116,6 +165,7 @@ void finish(plb_server* srv, Req* r, int state, const std::string& err) {
     r->t_done = srv->now();
     if (r->bytes) {
         srv->used -= r->bytes;
+        srv->active_cells -= cells_of(r);
         r->bytes = 0;
     }
     srv->done_cv.notify_all();
@@ -175,6 +225,18 @@ void fail_lane(plb_server* srv, Lane& L, const std::string& e) {
 }
 
 // Starts the next tick of an idle lane with members.
+// Lanes run on streams ranked by their work, so that small requests are not
+// held up behind large ones when the device is oversubscribed: batch lanes
+// (small requests) at the highest priority, solo lanes one level lower for
+// each factor of ~3 of cell updates above 3e8.
+int solo_priority(const plb_server* srv, const Req* r) {
+    const double w = (double)r->p.nx * r->p.ny * r->p.nz * (double)r->steps;
+    int level = w > 3e8 ? (int)(std::log10(w / 3e8) * 2.0) : 0;
+    const int levels = srv->prio_least - srv->prio_greatest;   // >= 0; larger number = lower priority
+    if (level > levels) level = levels;
+    return srv->prio_greatest + level;
+}
+
 void launch_tick(plb_server* srv, Lane& L) {
     if (!L.done && cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming) != cudaSuccess) {
         fail_lane(srv, L, "cudaEventCreate failed");
@@ -194,6 +256,8 @@ void launch_tick(plb_server* srv, Lane& L) {
             std::vector<plb_solve*> ss;
             for (Req* r : L.members) ss.push_back(r->s);
             if (plb_batch_create((int32_t)ss.size(), ss.data(), &L.batch) != PLB_OK)
+                return fail_lane(srv, L, plb_last_error());
+            if (plb::set_batch_priority(L.batch, srv->prio_greatest) != PLB_OK)
                 return fail_lane(srv, L, plb_last_error());
             L.dirty = false;
         }
@@ -232,6 +296,8 @@ bool collect_tick(plb_server* srv, Lane& L) {
 
 void scheduler(plb_server* srv) {
     cudaSetDevice(srv->device);
+    if (cudaDeviceGetStreamPriorityRange(&srv->prio_least, &srv->prio_greatest) != cudaSuccess)
+        srv->prio_least = srv->prio_greatest = 0;
     for (;;) {
         // 1. admission
         std::vector<Req*> admitted;
@@ -245,18 +311,31 @@ void scheduler(plb_server* srv) {
                 srv->work_cv.wait(lk, [&] { return srv->stop || !srv->pending.empty(); });
             if (srv->stop) break;
             while (!srv->pending.empty()) {
-                Req* r = srv->pending.front();
+                // the next request: the oldest when it has waited long enough
+                // (or in arrival order), else the one with the least work
+                size_t pick = 0;
+                const double tnow = srv->now();
+                if (!fifo_order() && tnow - srv->pending.front()->t_sub < max_wait_s()) {
+                    double best = work_of(srv->pending[0]);
+                    for (size_t i = 1; i < srv->pending.size(); ++i) {
+                        const double w = work_of(srv->pending[i]);
+                        if (w < best) { best = w; pick = i; }
+                    }
+                }
+                Req* r = srv->pending[pick];
                 const int64_t need = plb_solve_bytes(&r->p);
                 if (need > srv->budget) {
-                    srv->pending.pop_front();
+                    srv->pending.erase(srv->pending.begin() + (long)pick);
                     r->state = PLB_REQ_FAILED;
                     r->err = "request needs more device memory than the whole budget";
                     r->t_done = srv->now();
                     srv->done_cv.notify_all();
                     continue;
                 }
-                if (srv->used + need > srv->budget) break;   // wait for room, keep arrival order
-                srv->pending.pop_front();
+                if (srv->used + need > srv->budget) break;   // wait for room
+                if (srv->active_cells > 0 && srv->active_cells + cells_of(r) > active_cells_cap()) break;
+                srv->pending.erase(srv->pending.begin() + (long)pick);
+                srv->active_cells += cells_of(r);
                 srv->used += need;
                 if (srv->used > srv->peak) srv->peak = srv->used;
                 r->bytes = need;
@@ -274,6 +353,13 @@ void scheduler(plb_server* srv) {
             }
             // large solves, and AA ones (batches are AB only), run alone
             if (r->p.nx * r->p.ny * r->p.nz >= solo_cells() || r->p.streaming == PLB_STREAMING_AA) {
+                if (plb::set_solve_priority(r->s, solo_priority(srv, r)) != PLB_OK) {
+                    const std::string e2 = plb_last_error();
+                    plb_solve_destroy(r->s);
+                    r->s = nullptr;
+                    finish(srv, r, PLB_REQ_FAILED, e2);
+                    continue;
+                }
                 auto L = std::make_unique<Lane>();
                 L->solo = true;
                 L->members.push_back(r);

@@ -99,7 +99,7 @@ def main(argv=None):
     cell_updates = sum(np.prod(r["dims"]) * r["steps"] for r in reqs)
 
     # ---- served ------------------------------------------------------------------
-    lat, results = {}, {}
+    lat, waits, runs, results = {}, {}, {}, {}
     with capi.Server(budget_bytes=int(a.budget_gb * (1 << 30)), tick_steps=a.tick) as srv:
         ids = [None] * len(reqs)
         t0 = time.perf_counter()
@@ -118,11 +118,15 @@ def main(argv=None):
             srv.wait(ids[i], 3600.0)
             rho, u, (ts, tadm, tdone) = srv.result(ids[i])
             lat[i] = tdone - ts
+            waits[i] = tadm - ts
+            runs[i] = tdone - tadm
             if i < a.accuracy_sample:
                 results[i] = u
         t_served = time.perf_counter() - t0
         _, peak = srv.memory()
     lats = np.array([lat[i] for i in range(len(reqs))])
+    work = np.array([float(np.prod(r["dims"])) * r["steps"] for r in reqs])
+    small = work <= np.median(work)
 
     # ---- serial plain solves ---------------------------------------------------------
     nplain = len(reqs) if a.plain < 0 else min(a.plain, len(reqs))
@@ -148,6 +152,9 @@ def main(argv=None):
         "served_solves_per_s": round(served_rate, 3), "served_mlups": round(cell_updates / t_served / 1e6, 1),
         "latency_p50_s": round(float(np.percentile(lats, 50)), 3),
         "latency_p99_s": round(float(np.percentile(lats, 99)), 3), "peak_budget_bytes": int(peak),
+        "wait_p50_s": round(float(np.median([waits[i] for i in range(len(reqs))])), 3),
+        "run_p50_s": round(float(np.median([runs[i] for i in range(len(reqs))])), 3),
+        "latency_p50_smaller_half_s": round(float(np.percentile(lats[small], 50)), 3),
         "plain_requests": nplain, "plain_seconds": round(t_plain, 2), "plain_solves_per_s": round(plain_rate, 3),
         "speedup": round(served_rate / plain_rate, 2) if nplain else None,
         "u_rel_l2_vs_fp64": {k: [float(f"{x:.3g}") for x in v] for k, v in errs.items()},

@@ -11,14 +11,14 @@ DUCT = {"east": "periodic", "west": "periodic", "north": "noslip", "south": "nos
 REST = {f: (0.0, 0.0, 0.0) for f in ("north", "south", "up", "down")}
 
 
-def make_solves(capi, storage, seed=5, count=7, model="D3Q19"):
+def make_solves(capi, storage, seed=5, count=7, model="D3Q19", even_fp16=True):
     from plbpd_gb300.workloads import porous_mask
     rng = np.random.default_rng(seed)
     out = []
     for i in range(count):
         L = int(rng.integers(6, 30))
         nx, ny, nz = L + int(rng.integers(0, 5)), L, L + int(rng.integers(0, 3))
-        if storage == capi.STORAGE_FP16_DEV:
+        if storage == capi.STORAGE_FP16_DEV and even_fp16:
             nx += nx % 2
         tau = float(rng.uniform(0.55, 1.2))
         vel = dict(REST)
@@ -34,13 +34,18 @@ def make_solves(capi, storage, seed=5, count=7, model="D3Q19"):
     return out
 
 
-@pytest.mark.parametrize("storage_name", ["fp32", "fp16", "fp32dev"])
+@pytest.mark.parametrize("storage_name", ["fp32", "fp16", "fp16_odd", "fp32dev"])
 @pytest.mark.parametrize("model", ["D3Q19", "D3Q27"])
 def test_batch_equals_each_domain_alone(storage_name, model):
+    """Domains with even nx run as pair tasks, the others as one-node tasks,
+    in the same launch (fp16_odd: FP16 domains of both kinds)."""
     from plbpd_gb300 import capi
-    storage = {"fp32": capi.STORAGE_FP32, "fp16": capi.STORAGE_FP16_DEV, "fp32dev": capi.STORAGE_FP32_DEV}[storage_name]
-    mix = make_solves(capi, storage, model=model)
-    alone = make_solves(capi, storage, model=model)
+    storage = {"fp32": capi.STORAGE_FP32, "fp16": capi.STORAGE_FP16_DEV, "fp16_odd": capi.STORAGE_FP16_DEV,
+               "fp32dev": capi.STORAGE_FP32_DEV}[storage_name]
+    even = storage_name != "fp16_odd"
+    mix = make_solves(capi, storage, model=model, even_fp16=even)
+    alone = make_solves(capi, storage, model=model, even_fp16=even)
+    assert len({s.nx % 2 for s in mix}) == (1 if storage_name == "fp16" else 2)
     with capi.Batch(mix) as b:
         b.step(1)       # first collision from the initial state
         b.step(140)     # graph chunks plus a tail

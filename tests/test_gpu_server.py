@@ -143,12 +143,12 @@ def test_cancel_queued_and_running_requests():
     budget = int(capi.lib().plb_solve_bytes(capi.C.byref(big_p)) * 1.2)
     with capi.Server(budget_bytes=budget, tick_steps=20) as srv:
         running = srv.submit(big_p, 2_000_000, big_m)      # holds the budget
-        queued = srv.submit(big_p, 50, big_m)              # waits for it
         for _ in range(2000):
             if srv.status(running) == capi.REQ_RUNNING:
                 break
             time.sleep(0.005)
         assert srv.status(running) == capi.REQ_RUNNING
+        queued = srv.submit(big_p, 50, big_m)              # waits for it
         assert srv.status(queued) == capi.REQ_QUEUED
         srv.cancel(queued)
         assert srv.status(queued) == capi.REQ_CANCELLED
@@ -200,3 +200,26 @@ def test_failing_client_does_not_disturb_others():
     for k in range(1, len(reqs)):
         p, m, n = reqs[k]
         assert np.array_equal(out[k].view(np.uint32), run_alone(capi, p, m, n)[1].view(np.uint32))
+
+
+def test_smaller_requests_are_admitted_first():
+    """With the budget taken, the queued request with the least work is
+    admitted first when room frees up (not the oldest)."""
+    from plbpd_gb300 import capi
+    rng = np.random.default_rng(21)
+    p, m, _ = request_params(capi, rng, "D3Q19", capi.STORAGE_FP32)
+    budget = int(capi.lib().plb_solve_bytes(capi.C.byref(p)) * 1.5)   # one at a time
+    with capi.Server(budget_bytes=budget, tick_steps=20) as srv:
+        first = srv.submit(p, 400, m)
+        for _ in range(2000):
+            if srv.status(first) == capi.REQ_RUNNING:
+                break
+            time.sleep(0.005)
+        long_one = srv.submit(p, 300, m)     # older, more work
+        short_one = srv.submit(p, 30, m)     # newer, less work
+        for rid in (first, long_one, short_one):
+            srv.wait(rid, 300.0)
+        t_long = srv.result(long_one)[2]
+        t_short = srv.result(short_one)[2]
+        srv.result(first)
+    assert t_short[1] <= t_long[1]           # admitted first
