@@ -142,8 +142,8 @@ struct BatchDomain {
 // One launch advances every domain by one step, reading f[parity] and
 // writing f[parity ^ 1]; `blocks` resident blocks walk the task list.
 // `moving`: some member has a moving wall.
-// `pairs`: FP16 storage, every domain's nx even, tasks of 64 nodes: the pair
-// kernel's work.
+// `pairs`: the task list holds 64-node pair tasks (task .w = 1, domains with
+// even nx: the two-node pair kernel's work) beside 32-node one-node tasks.
 int nat_batch_step(int q, int storage, int arith, bool moving, bool pairs, const BatchDomain* doms,
                    const int4* tiles, int ntiles, int parity, int blocks, cudaStream_t st);
 // Resident blocks per SM of the batch kernel (for sizing the grid).
