@@ -204,9 +204,11 @@ int plb_synchronize(plb_solve* s);
 void* plb_stream_handle(plb_solve* s);
 
 /* ---- kernel autotuning ----------------------------------------------------------
- * The FP16 pair kernel (NATIVE semantics, FP16 storage, even nx) comes in
- * several compiled variants that give bit-identical results.  Before a
- * solve's first fused step the library times each on the solve's own buffers
+ * The NATIVE fused step with even nx comes in several compiled variants that
+ * give bit-identical results: for FP16 storage seven forms of the two-node
+ * pair kernel, for FP32 (FP32 arithmetic) and FP32_DEV storage the one-node
+ * kernel and three forms of the pair kernel.  Before a solve's first fused
+ * step the library times each on the solve's own buffers
  * (the trial steps write only the buffer the next step overwrites) and keeps
  * the fastest per lattice, storage, collision, mask, block width and size
  * class (floor(log2 cells)) for the process; PLB_TUNE_CACHE=<file> keeps the
