@@ -61,7 +61,9 @@ static void FN(collide_node)(const orc_sim* s, R* nl, R rho, const R* ul, R drho
     }
 #else
     const float tau = s->tau, omega = s->omega;
-    const float tau_rhoinv = tau / rho;
+    /* the deviation form (FP16/FP32 deviation storage) takes tau (1/rho), one
+     * reciprocal shared with the moments; plbpd's FP32 forms take tau/rho */
+    const float tau_rhoinv = (orc_dev(s) && !s->trt) ? tau * (1.0f / rho) : tau / rho;
     float uu[3];
     for (int i = 0; i < 3; ++i) uu[i] = ul[i] + s->force[i] * tau_rhoinv;
     const float usq = uu[0] * uu[0] + uu[1] * uu[1] + uu[2] * uu[2];

@@ -237,7 +237,9 @@ template <int Q, bool DEV, int SC = 0>
 __device__ __forceinline__ void collide_node_trt(float (&f)[Q], float drho, float rho, float ux, float uy, float uz,
                                                  const CollideParams& P) {
     constexpr float S = pow2f(SC);
-    const float hr = __fdiv_rn(0.5f, rho);
+    // 0.5 (1/rho) is 0.5/rho exactly (a power-of-2 factor), and 1/rho is the
+    // moments' reciprocal, which the compiler shares
+    const float hr = __fmul_rn(0.5f, __fdiv_rn(1.0f, rho));
     const float vx = __fadd_rn(ux, __fmul_rn(P.fx, hr));
     const float vy = __fadd_rn(uy, __fmul_rn(P.fy, hr));
     const float vz = __fadd_rn(uz, __fmul_rn(P.fz, hr));

@@ -124,7 +124,8 @@ struct Nbr {
 template <int Q, int SC = 0>
 __device__ __forceinline__ void collide_node_dev(float (&d)[Q], float drho, float rho, float ux, float uy,
                                                  float uz, const CollideParams& P) {
-    const float tr = __fdiv_rn(P.tau, rho);
+    // tau (1/rho): the reciprocal is the moments' (the compiler shares it)
+    const float tr = __fmul_rn(P.tau, __fdiv_rn(1.0f, rho));
     const float vx = __fadd_rn(ux, __fmul_rn(P.fx, tr));
     const float vy = __fadd_rn(uy, __fmul_rn(P.fy, tr));
     const float vz = __fadd_rn(uz, __fmul_rn(P.fz, tr));
@@ -429,7 +430,7 @@ template <int Q, bool NEG, int SC>
 __device__ __forceinline__ void collide_node_dev2(float2 (&d)[Q], float2 drho, float2 rho, float2 ux, float2 uy,
                                                   float2 uz, const CollideParams& P) {
     const float2 nz = bc2(P.neg_zero);
-    const float2 tr = div2(P.tau, rho);
+    const float2 tr = mul2(bc2(P.tau), div2(1.0f, rho));   // tau (1/rho), as collide_node_dev
     Vel2 u;
     float2 (&v)[3] = u.v;
     v[0] = add2(ux, mulx2(bc2(P.fx), tr, nz));
@@ -467,7 +468,7 @@ template <int Q, int SC>
 __device__ __forceinline__ void collide_node_trt_dev2(float2 (&f)[Q], float2 drho, float2 rho, float2 ux, float2 uy,
                                                       float2 uz, const CollideParams& P) {
     const float2 nz = bc2(P.neg_zero);
-    const float2 hr = div2(0.5f, rho);
+    const float2 hr = mul2(bc2(0.5f), div2(1.0f, rho));   // = 0.5/rho exactly (power-of-2 factor)
     Vel2 u;
     u.v[0] = add2(ux, mulx2(bc2(P.fx), hr, nz));
     u.v[1] = add2(uy, mulx2(bc2(P.fy), hr, nz));
