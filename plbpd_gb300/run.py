@@ -41,6 +41,8 @@ def params_for(a):
           "fp64": capi.STORAGE_FP64}[a.storage]
     ar = capi.ARITH_REFERENCE if a.arith == "reference" else capi.ARITH_FP32
     col = dict(collision=capi.COLLISION_TRT if a.collision == "trt" else capi.COLLISION_BGK)
+    if getattr(a, "streaming", "ab") == "aa":
+        col["streaming"] = capi.STREAMING_AA
     nu = nu_for_tau(a.tau)
     if a.workload == "periodic":
         faces = {f: "periodic" for f in capi.FACES}
@@ -77,6 +79,8 @@ def main(argv=None):
     ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16", "fp32dev", "fp64"])
     ap.add_argument("--collision", default="bgk", choices=["bgk", "trt"])
     ap.add_argument("--arith", default="fp32", choices=["fp32", "reference"])
+    ap.add_argument("--streaming", default="ab", choices=["ab", "aa"],
+                    help="two population buffers (ab) or one updated in place (aa)")
     a = ap.parse_args(argv)
     p = params_for(a)
     cells = int(p.nx) * int(p.ny) * int(p.nz)
@@ -91,7 +95,8 @@ def main(argv=None):
         s.step(a.steps)
         dt = time.perf_counter() - t0
         print(json.dumps({"workload": a.workload, "model": a.model, "dims": [int(p.nx), int(p.ny), int(p.nz)],
-                          "storage": a.storage, "arith": a.arith, "spheres": a.spheres, "steps": a.steps,
+                          "storage": a.storage, "arith": a.arith, "streaming": a.streaming, "spheres": a.spheres,
+                          "steps": a.steps,
                           "seconds": round(dt, 4), "mlups": round(cells * a.steps / dt / 1e6, 1),
                           "mass": s.conservation()[0], "device_bytes": s.device_bytes(), "variant": s.variant()}))
 
