@@ -404,9 +404,11 @@ int ref_materialize_fields(plb_solve* s) {
 }
 
 // ---- autotuner of the fused-step kernel --------------------------------------
-// The FP16 pair kernel is compiled in several variants that give the same
-// bits (native_impl.cuh, kH2Variant); which is fastest depends on the
-// lattice, the mask, the block width and the domain size.  Before a solve's
+// The NATIVE fused step with even nx is compiled in several variants that
+// give the same bits (native_impl.cuh: kH2Variant for FP16 storage; the
+// one-node kernel and the pair kernel's forms for FP32 and FP32_DEV); which
+// is fastest depends on the lattice, the mask, the block width and the
+// domain size.  Before a solve's
 // first fused step the variants are timed on the solve's own buffers: a pull
 // step reads buffer cur and writes the other one, which the next real step
 // overwrites, so trial launches leave the state as it was.  The winner is
