@@ -41,6 +41,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/plb.h"
+#include "admission.h"
 
 namespace plb {
 void record_error(const std::string& msg);   // capi.cu: the plb_last_error() slot
@@ -310,31 +311,33 @@ void scheduler(plb_server* srv) {
             if (!busy)
                 srv->work_cv.wait(lk, [&] { return srv->stop || !srv->pending.empty(); });
             if (srv->stop) break;
+            plb::AdmissionState ast;
+            ast.budget = srv->budget;
+            ast.cap_cells = active_cells_cap();
+            ast.max_wait = max_wait_s();
+            ast.fifo = fifo_order();
+            std::vector<plb::AdmissionView> view;
+            for (const Req* q : srv->pending)
+                view.push_back({q->t_sub, work_of(q), cells_of(q), plb_solve_bytes(&q->p)});
             while (!srv->pending.empty()) {
-                // the next request: the oldest when it has waited long enough
-                // (or in arrival order), else the one with the least work
-                size_t pick = 0;
-                const double tnow = srv->now();
-                if (!fifo_order() && tnow - srv->pending.front()->t_sub < max_wait_s()) {
-                    double best = work_of(srv->pending[0]);
-                    for (size_t i = 1; i < srv->pending.size(); ++i) {
-                        const double w = work_of(srv->pending[i]);
-                        if (w < best) { best = w; pick = i; }
-                    }
-                }
+                ast.used = srv->used;
+                ast.active_cells = srv->active_cells;
+                const size_t pick = plb::admission_pick(view, ast, srv->now());
                 Req* r = srv->pending[pick];
-                const int64_t need = plb_solve_bytes(&r->p);
-                if (need > srv->budget) {
+                const int64_t need = view[pick].bytes;
+                const plb::Admit what = plb::admission_decide(view[pick], ast);
+                if (what == plb::Admit::kReject) {
                     srv->pending.erase(srv->pending.begin() + (long)pick);
+                    view.erase(view.begin() + (long)pick);
                     r->state = PLB_REQ_FAILED;
                     r->err = "request needs more device memory than the whole budget";
                     r->t_done = srv->now();
                     srv->done_cv.notify_all();
                     continue;
                 }
-                if (srv->used + need > srv->budget) break;   // wait for room
-                if (srv->active_cells > 0 && srv->active_cells + cells_of(r) > active_cells_cap()) break;
+                if (what == plb::Admit::kWait) break;   // wait for room
                 srv->pending.erase(srv->pending.begin() + (long)pick);
+                view.erase(view.begin() + (long)pick);
                 srv->active_cells += cells_of(r);
                 srv->used += need;
                 if (srv->used > srv->peak) srv->peak = srv->used;
