@@ -44,6 +44,10 @@ SEED = 20261203
 N_SIDE = 256
 Q = 19
 BYTES_PER_CELL = 2 * Q * 4          # one read and one write of every FP32 population
+# --storage: FP32 (the default and the headline), FP16 deviations (2 B a
+# population) or FP32 deviations; name, bytes per cell update
+STORAGES = {"fp32": ("STORAGE_FP32", 2 * Q * 4), "fp16": ("STORAGE_FP16_DEV", 2 * Q * 2),
+            "fp32dev": ("STORAGE_FP32_DEV", 2 * Q * 4)}
 TAU = 0.6
 PERIODIC = {f: "periodic" for f in ("east", "west", "north", "south", "up", "down")}
 WORKLOAD = "D3Q19 BGK 256^3, tau 0.6, fully periodic, Taylor-Green A=0.02 + noise, FP32"
@@ -280,7 +284,7 @@ def run_gpu_arm(args):
     nu = nu_for_tau(TAU)
     params = capi.make_params("D3Q19", N_SIDE, N_SIDE, N_SIDE, nu, rho0=1.0, face_type=PERIODIC,
                               semantics=capi.SEMANTICS_NATIVE, arith=capi.ARITH_FP32,
-                              storage=capi.STORAGE_FP32, device=local)
+                              storage=getattr(capi, STORAGES[args.storage][0]), device=local)
     cells = N_SIDE ** 3
     full = (N_SIDE + 2,) * 3
     pin_n = capi.PinnedBuffer(full + (Q,))
@@ -352,23 +356,27 @@ def run_gpu_arm(args):
     if rank != 0:
         return 0
     peak, peak_kind = measured_peak()
-    achieved = BYTES_PER_CELL * cells / (kms * 1e-3) / 1e9
-    traffic = read_traffic(variant)
+    bytes_per_cell = STORAGES[args.storage][1]
+    achieved = bytes_per_cell * cells / (kms * 1e-3) / 1e9
+    traffic = read_traffic(variant) if args.storage == "fp32" else None
     cs = clk.summary() or clk2.summary()
     line = {
         "metric": "MLUPS", "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "lattice": "D3Q19", "cells": cells, "tau": TAU,
-                   "boundaries": "periodic x/y/z", "storage": "fp32", "semantics": "native",
+        "config": {"workload": WORKLOAD if args.storage == "fp32" else WORKLOAD.replace(
+                       "FP32", {"fp16": "FP16 storage of f - w", "fp32dev": "FP32 storage of f - w"}[args.storage]),
+                   "lattice": "D3Q19", "cells": cells, "tau": TAU,
+                   "boundaries": "periodic x/y/z", "storage": args.storage, "semantics": "native",
                    "l2": "no flush: populations 2.7 GB > 129 MB L2", "parallelism": f"replicas x{world}",
                    "e2e": f"{e2e_iters} x (upload n/rho/u, {args.steps} steps, read rho/u)"},
         "e2e": {"value": round(e2e_val, 1), "unit": "MLUPS", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": VARIANT_KERNEL.get(variant, f"variant {variant}"), "variant": variant,
-                     "bytes_per_cell": BYTES_PER_CELL, "kernel_ms": round(kms, 4)},
+                     "kernel": (VARIANT_KERNEL.get(variant, f"variant {variant}") if args.storage == "fp32"
+                                else f"fused step, {args.storage} storage, autotuner variant {variant}"),
+                     "variant": variant, "bytes_per_cell": bytes_per_cell, "kernel_ms": round(kms, 4)},
         "gpu_launches": int(args.steps),
         "clocks": cs,
         "mass_after": mass,
@@ -389,6 +397,8 @@ def main(argv=None):
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--e2e-iters", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--storage", choices=sorted(STORAGES), default="fp32",
+                    help="population storage of the GPU arm (default fp32, the headline)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
