@@ -7,10 +7,12 @@ square grid of edge log-uniform in [64, 2048], 40% D3Q19 with a cube of edge
 log-uniform in [32, 160]; FP32 (f - w by default) or FP16 storage 50/50; tau uniform in
 [0.55, 1.5]; random 2x2x2 obstacles at 0-20% solid; 500-5000 steps; periodic
 x, resting walls on the other moving axes, a body force.  The server admits
-by device bytes under --budget-gb.  Printed: solves/s and p50/p99 latency
-(arrival to result) of the server, solves/s of the same requests run one
-after another as plain solves, and the relative L2 error of u against an
-FP64 run for a sample of the requests.
+by device bytes under --budget-gb (and by its own running-cells cap and
+smallest-work-first order).  Printed: solves/s and p50/p99 latency (arrival
+to result) of the server, the median wait for admission and run time, the
+median latency of the smaller half of the requests, solves/s of the same
+requests run one after another as plain solves, and the relative L2 error of
+u against an FP64 run for a sample of the requests.
 """
 from __future__ import annotations
 
