@@ -110,3 +110,24 @@ def test_tune_force_range(lib):
         assert e.value.code == capi.EINVAL
     capi.tune_force(0)
     capi.tune_force(-1)
+
+
+def test_solve_bytes_follow_storage_and_streaming(lib):
+    """plb_solve_bytes (the server's admission measure, host arithmetic only):
+    FP16 populations take half FP32's bytes, AA streaming one buffer instead
+    of two, FP64 twice FP32's."""
+    from plbpd_gb300 import capi
+
+    def nbytes(**kw):
+        p = capi.make_params("D3Q19", 64, 64, 64, 0.1, semantics=capi.SEMANTICS_NATIVE, arith=capi.ARITH_FP32,
+                             face_type={f: "periodic" for f in capi.FACES}, **kw)
+        return lib.plb_solve_bytes(capi.C.byref(p))
+
+    pop = 64 ** 3 * 19
+    fp32, fp16, fp64 = (nbytes(storage=capi.STORAGE_FP32), nbytes(storage=capi.STORAGE_FP16_DEV),
+                        nbytes(storage=capi.STORAGE_FP64))
+    aa = nbytes(storage=capi.STORAGE_FP32, streaming=capi.STREAMING_AA)
+    assert fp32 - fp16 == 2 * pop * 2          # two buffers, 2 bytes a population less
+    assert fp64 - fp32 == 2 * pop * 4
+    assert fp32 - aa == pop * 4                # one buffer fewer
+    assert min(fp32, fp16, fp64, aa) > 0
