@@ -231,8 +231,12 @@ int plb_tune_variant(const plb_solve* s, int32_t* variant);
  * own extents, tau, force, walls and mask, and its result is bit-identical
  * to advancing it alone.  The batch does not own its solves; their own entry
  * points (initialize, set/get field, set mask, conservation) still apply
- * between batch calls.  No counterpart in plbpd, which runs one problem per
- * process. */
+ * between batch calls, and each member's stream waits for the batch's work
+ * of the last call, so they see its result without plb_batch_synchronize.
+ * A batch keeps the kernel chosen at creation: after a member's lattice
+ * arithmetic or collision changes (plb_set_collision) or it gains a moving
+ * wall, plb_batch_step refuses with PLB_ESTATE; create a new batch.
+ * No counterpart in plbpd, which runs one problem per process. */
 typedef struct plb_batch plb_batch;
 int plb_batch_create(int32_t n, plb_solve* const* solves, plb_batch** out);
 int plb_batch_step(plb_batch* b, int64_t nsteps);

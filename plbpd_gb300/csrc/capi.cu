@@ -1131,6 +1131,8 @@ struct plb_batch {
     bool pairs = false;    // some domain has even nx: 64-node pair tasks beside 32-node ones
     int graph_steps = 64;
     cudaGraphExec_t graph = nullptr;
+    cudaEvent_t done = nullptr;   // recorded after each batch call's work
+    std::vector<cudaEvent_t> member_ev;   // one per member: its own work so far
     std::vector<BatchDomain> h_doms;
 };
 
@@ -1139,6 +1141,9 @@ namespace {
 void batch_release(plb_batch* b) {
     if (!b) return;
     if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->done) cudaEventDestroy(b->done);
+    for (cudaEvent_t e : b->member_ev)
+        if (e) cudaEventDestroy(e);
     if (b->d_doms) cudaFreeAsync(b->d_doms, b->stream);
     if (b->d_tiles) cudaFreeAsync(b->d_tiles, b->stream);
     if (b->stream) {
@@ -1168,6 +1173,21 @@ int batch_prepare(plb_batch* b, int64_t* consumed) {
         s->cur = 1 - s->cur;
     }
     *consumed = 1;
+    return PLB_OK;
+}
+
+// The batch's kernel was chosen for the lattice, storage, kernel arithmetic
+// (collision operator included) and moving walls its members had when it was
+// created; a member changed since then (plb_set_collision, new faces) would
+// run under the wrong kernel, so the call is refused instead.
+int batch_check_members(const plb_batch* b) {
+    for (const plb_solve* s : b->solves) {
+        if (s->q != b->q || s->storage != b->storage || s->karith != b->arith || s->aa || !s->native)
+            return fail(PLB_ESTATE, "a batch member's lattice, storage, arithmetic or collision changed after "
+                                    "plb_batch_create; create a new batch");
+        if (s->np.moving && !b->moving)
+            return fail(PLB_ESTATE, "a batch member gained a moving wall after plb_batch_create; create a new batch");
+    }
     return PLB_OK;
 }
 
@@ -1244,6 +1264,14 @@ int plb_batch_create(int32_t n, plb_solve* const* solves, plb_batch** out) {
         batch_release(b);
         return fail(PLB_ECUDA, "cudaStreamCreate");
     }
+    b->member_ev.assign(n, nullptr);
+    bool ev_ok = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i < n && ev_ok; ++i)
+        ev_ok = cudaEventCreateWithFlags(&b->member_ev[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!ev_ok) {
+        batch_release(b);
+        return fail(PLB_ECUDA, "cudaEventCreate");
+    }
     // a domain with even nx runs as pair tasks (two nodes a lane, 64 a warp)
     std::vector<int4> tiles;
     for (int i = 0; i < n; ++i) {
@@ -1283,7 +1311,12 @@ int plb_batch_step_async(plb_batch* b, int64_t nsteps) {
     if (nsteps < 0) return fail(PLB_EINVAL, "negative step count");
     if (nsteps == 0) return PLB_OK;
     PLB_CUDA(cudaSetDevice(b->device));
-    for (plb_solve* s : b->solves) PLB_TRY(sync(s));   // members' own work comes first
+    PLB_TRY(batch_check_members(b));
+    // members' own work comes first (stream order, no host wait)
+    for (size_t m = 0; m < b->solves.size(); ++m) {
+        PLB_CUDA(cudaEventRecord(b->member_ev[m], b->solves[m]->stream));
+        PLB_CUDA(cudaStreamWaitEvent(b->stream, b->member_ev[m], 0));
+    }
     int64_t done = 0;
     PLB_TRY(batch_prepare(b, &done));
     PLB_TRY(batch_upload_table(b));
@@ -1300,6 +1333,10 @@ int plb_batch_step_async(plb_batch* b, int64_t nsteps) {
                                   b->blocks, b->stream));
     if (todo & 1)
         for (plb_solve* s : b->solves) s->cur = 1 - s->cur;
+    // a member's own calls (fields, conservation, steps) run on its stream:
+    // order them after the batch's work on its buffers
+    PLB_CUDA(cudaEventRecord(b->done, b->stream));
+    for (plb_solve* s : b->solves) PLB_CUDA(cudaStreamWaitEvent(s->stream, b->done, 0));
     return PLB_OK;
 }
 

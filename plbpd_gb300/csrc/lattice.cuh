@@ -11,6 +11,8 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include "tail_exact.h"
+
 namespace plb {
 
 // ---------------------------------------------------------------------------
@@ -214,7 +216,8 @@ __device__ __forceinline__ float dot_c(int k, float ux, float uy, float uz) {
 //         neq = (neq*rho)*w;  n = fma(1-omega, n, omega*neq)
 //   tail (k >= 8*floor(Q/8), REFERENCE arithmetic only): the bracket
 //         1 + 3cu + 4.5cu^2 - 1.5usq in FP64 times the float w*rho, then
-//         (1-omega)*n (float) + omega*neq in FP64, rounded to float.
+//         (1-omega)*n (float) + omega*neq in FP64, rounded to float; the
+//         result is formed from FP32 instructions (tail_exact.h).
 // ---- TRT ----------------------------------------------------------------------
 // Two relaxation times with a second-order force source (the oracle's
 // orc_set_trt states the method); pairs (k, k + 1) with k odd are opposite
@@ -294,6 +297,7 @@ __device__ __forceinline__ void collide_node(float (&f)[Q], float rho, float ux,
     const float kusq = __fmul_rn(-1.5f, usq);
     const float om = P.omega, omc = P.omc;
     constexpr int kBody = (ARITH == kArithReference) ? (Q / 8) * 8 : Q;
+    const tx::TailNode tnode = tx::tail_node(usq);
 #pragma unroll
     for (int k = 0; k < Q; ++k) {
         const float cu = (k == 0) ? 0.0f : dot_c<Q>(k, vx, vy, vz);
@@ -306,16 +310,12 @@ __device__ __forceinline__ void collide_node(float (&f)[Q], float rho, float ux,
             neq = __fmul_rn(neq, weight<Q>(k));
             f[k] = __fmaf_rn(omc, f[k], __fmul_rn(om, neq));
         } else {
+            // the reference's double-precision tail, reproduced bit for bit
+            // from FP32 instructions (tail_exact.h); the rare lanes whose
+            // result lies too close to a rounding boundary run it in FP64
             const float wr = __fmul_rn(weight<Q>(k), rho);
-            const double cud = (double)cu;
-            // 3*cu, 4.5*cu and (4.5*cu)*cu are exact in double, so each sum
-            // rounds once, as in the reference's expression.
-            double br = __dadd_rn(1.0, __dmul_rn(3.0, cud));
-            br = __dadd_rn(br, __dmul_rn(__dmul_rn(4.5, cud), cud));
-            br = __dsub_rn(br, __dmul_rn(1.5, (double)usq));
-            const double neq = __dmul_rn((double)wr, br);
             const float a = __fmul_rn(omc, f[k]);
-            f[k] = __double2float_rn(__dadd_rn((double)a, __dmul_rn((double)om, neq)));
+            f[k] = tx::tail_update(cu, usq, tnode, wr, om, a);
         }
     }
 }

@@ -82,3 +82,37 @@ def test_batch_rejects_mixed_lattices():
                           semantics=capi.SEMANTICS_NATIVE)
     with pytest.raises(capi.PlbError):
         capi.Batch([a, b])
+
+
+def test_batch_refuses_member_with_changed_collision():
+    """The batch's kernel is fixed at creation: a member switched from BGK to
+    TRT afterwards is refused, not run under the BGK kernel."""
+    from plbpd_gb300 import capi
+    mix = make_solves(capi, capi.STORAGE_FP32, seed=11, count=3)
+    with capi.Batch(mix) as b:
+        b.step(4)
+        mix[1].set_collision(capi.COLLISION_TRT)
+        with pytest.raises(capi.PlbError) as e:
+            b.step(2)
+        assert e.value.code == capi.ESTATE
+        mix[1].set_collision(capi.COLLISION_BGK)
+        b.step(2)   # back to the batch's operator: accepted
+
+
+def test_member_calls_follow_batch_without_synchronize():
+    """A member's own calls after plb_batch_step_async see the batch's result
+    (its stream waits for the batch's work), with no plb_batch_synchronize."""
+    from plbpd_gb300 import capi
+    mix = make_solves(capi, capi.STORAGE_FP32, seed=13, count=3)
+    alone = make_solves(capi, capi.STORAGE_FP32, seed=13, count=3)
+    with capi.Batch(mix) as b:
+        b.step_async(1)
+        b.step_async(130)
+        got = [m.get(capi.FIELD_U) for m in mix]
+        cons = [m.conservation() for m in mix]
+        b.synchronize()
+    for s in alone:
+        s.step(131)
+    for a, g, c in zip(alone, got, cons):
+        assert np.array_equal(a.get(capi.FIELD_U).view(np.uint32), g.view(np.uint32))
+        np.testing.assert_array_equal(a.conservation(), c)
