@@ -345,7 +345,10 @@ int plb_conservation(plb_solve* s, double* out4);
  * Block partials live in a fixed 128 KiB __device__ array inside the library,
  * so ncells is limited to 16,777,216 (PLB_EINVAL beyond).  The first call on
  * a device looks that array's address up (cudaGetSymbolAddress, with the
- * device current); make that first call before any stream capture.  All calls
+ * device current) and keeps it for the life of the process; make that first
+ * call before any stream capture.  The address belongs to the device's
+ * context: after cudaDeviceReset on that device it is stale, so a process that
+ * resets a device must not call this entry point on it again.  All calls
  * share the array: calls whose kernels overlap on the GPU race on it. */
 int plb_conservation_static(int32_t q, const float* n, int64_t ncells, int64_t plane_stride,
                             const uint8_t* solid, double* out4, void* stream);

@@ -40,6 +40,39 @@ DUCT = {"east": "periodic", "west": "periodic", "north": "noslip", "south": "nos
 REST = {f: (0.0, 0.0, 0.0) for f in ("north", "south", "up", "down")}
 
 
+def poiseuille_startup(zeta, t: float, nu: float, g: float, h: float, terms: int = 4001) -> np.ndarray:
+    """Plane Poiseuille flow started from rest: the velocity at distance zeta
+    from one wall of a channel of width h, t time units after an acceleration
+    g is switched on (kinematic viscosity nu).  The series solution of the
+    diffusion equation with no-slip walls:
+        u = g h^2 / (2 nu) [ (zeta/h)(1 - zeta/h)
+                             - sum_{n odd} 8/(n pi)^3 sin(n pi zeta/h) exp(-(n pi)^2 nu t / h^2) ]"""
+    zeta = np.asarray(zeta, np.float64)
+    x = zeta / h
+    s = x * (1.0 - x)
+    for n in range(1, terms, 2):
+        a = (n * np.pi) ** 2 * nu * t / (h * h)
+        if a > 700.0:
+            break
+        s = s - 8.0 / (n * np.pi) ** 3 * np.sin(n * np.pi * x) * np.exp(-a)
+    return g * h * h / (2.0 * nu) * s
+
+
+def channel_profile_error(u: np.ndarray, steps: int, nu: float, force: float) -> float:
+    """Relative L2 error of the x-averaged velocity profile of a body-force
+    driven channel (plbpd's field layout (nz+2, ny+2, nx+2, 3), wall layers on
+    the first and last interior z layers, half-way walls 1.5 and nz + 0.5)
+    against poiseuille_startup.  plbpd's velocity is the moment sum c f / rho
+    (src/CalcMoments.hpp:28-36), which the forcing scheme (u + F tau / rho in
+    the equilibrium) leaves half a force step behind the fluid velocity, so
+    F/2 is added before comparing."""
+    nz = u.shape[0] - 2
+    prof = np.asarray(u[2:nz, 1, 1:-1, 0], np.float64).mean(axis=1) + 0.5 * force
+    zeta = np.arange(2, nz, dtype=np.float64) - 1.5
+    ref = poiseuille_startup(zeta, float(steps), nu, force, float(nz - 2))
+    return float(np.linalg.norm(prof - ref) / np.linalg.norm(ref))
+
+
 def wall_layers(faces: dict, nx: int, ny: int, nz: int) -> np.ndarray:
     solid = np.zeros((nz, ny, nx), bool)
     if faces.get("east") == "noslip": solid[:, :, -1] = True

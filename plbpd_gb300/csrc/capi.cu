@@ -338,7 +338,22 @@ int validate(const plb_params* p) {
 // cudaHostAlloc, registered memory) is read or written by the layout kernels
 // directly over the host link: one pass instead of a copy plus a pass.
 // Returns null for other memory, which goes through the staging buffer.
+// Page-locked host memory can be read and written by the layout kernels in
+// place over the host link (PLB_PINNED_TRANSFER=direct), or moved by one
+// bulk DMA copy through the device staging buffer with the layout conversion
+// on the device (copy, the default: on GB300 the copy engines move a large
+// pinned buffer several times faster than kernel loads and stores that cross
+// the link).  Other host memory always takes the staging path.
+bool pinned_direct() {
+    static const bool direct = [] {
+        const char* e = std::getenv("PLB_PINNED_TRANSFER");
+        return e && std::strcmp(e, "direct") == 0;
+    }();
+    return direct;
+}
+
 float* device_view(const void* host) {
+    if (!pinned_direct()) return nullptr;
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
         cudaGetLastError();

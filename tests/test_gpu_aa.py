@@ -1,12 +1,14 @@
-"""AA in-place streaming (one population buffer) against the two-buffer
-kernels, bit for bit: every storage, both collision operators, odd and even
-step counts (the buffer's two layouts), graph chunks, reads and writes of the
-state between steps, and half the population memory."""
+"""AA in-place streaming (one population buffer) against the oracle and
+against the two-buffer kernels, bit for bit: every storage, both collision
+operators, odd and even step counts (the buffer's two layouts), graph chunks,
+reads and writes of the state between steps, and half the population
+memory."""
 import numpy as np
 import pytest
 
+import pyoracle as po
 from conftest import assert_bitexact
-from test_gpu_native import NATIVE_CASES, mask_for
+from test_gpu_native import NATIVE_CASES, compare, mask_for
 
 pytestmark = pytest.mark.gpu
 
@@ -91,3 +93,33 @@ def test_aa_refused_where_undefined():
         capi.Solve.create(**CASES["d2q9_channel"], streaming=capi.STREAMING_AA)
     with make(capi, "torus_d3q19", "fp32", capi.STREAMING_AA, 0) as aa, pytest.raises(capi.PlbError):
         capi.Batch([aa])
+
+
+ORACLE_MODE = {"fp32": dict(arith=po.ARITH_FP32), "fp16": dict(arith=po.ARITH_FP16DEV), "fp64": dict(precision=1),
+               "fp32dev": dict(arith=po.ARITH_FP32DEV)}
+
+
+@pytest.mark.parametrize("collision", ["bgk", "trt"])
+@pytest.mark.parametrize("storage", STORAGES)
+@pytest.mark.parametrize("case", sorted(NATIVE_CASES))
+def test_aa_matches_oracle(case, storage, collision):
+    """AA against the oracle's restatement directly (the oracle has no AA:
+    its two-buffer pull step is the definition the in-place update must
+    reproduce)."""
+    from plbpd_gb300 import capi
+    cfg = NATIVE_CASES[case]
+    mask = mask_for(case, cfg)
+    kw = dict(ORACLE_MODE[storage])
+    if collision == "trt":
+        kw["trt"] = 0.0
+    p = po.Port(**cfg, mode=po.MODE_NATIVE, mask=mask, **kw)
+    p._cfg = cfg
+    p.initialize()
+    col = capi.COLLISION_TRT if collision == "trt" else capi.COLLISION_BGK
+    with make(capi, case, storage, capi.STREAMING_AA, col) as aa:
+        done = 0
+        for target in (1, 2, 7, 150):      # odd counts end in the swapped layout
+            p.step(target - done)
+            aa.step(target - done)
+            done = target
+            compare(aa, p, mask, f"AA {case} {storage} {collision} step {target}")
