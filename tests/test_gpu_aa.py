@@ -8,7 +8,7 @@ import pytest
 
 import pyoracle as po
 from conftest import assert_bitexact
-from test_gpu_native import NATIVE_CASES, compare, mask_for
+from test_gpu_native import NATIVE_CASES, compare, mask_for, perturbed_start
 
 pytestmark = pytest.mark.gpu
 
@@ -115,8 +115,14 @@ def test_aa_matches_oracle(case, storage, collision):
     p = po.Port(**cfg, mode=po.MODE_NATIVE, mask=mask, **kw)
     p._cfg = cfg
     p.initialize()
+    # the same non-uniform float start on both sides (FP64 storage computes
+    # its initial equilibrium with the exact weights, the oracle's with
+    # plbpd's float ones)
+    n, rho, u = perturbed_start(p, 17)
+    p.set(po.N, n); p.set(po.RHO, rho); p.set(po.U, u)
     col = capi.COLLISION_TRT if collision == "trt" else capi.COLLISION_BGK
     with make(capi, case, storage, capi.STREAMING_AA, col) as aa:
+        aa.set(0, n); aa.set(2, rho); aa.set(3, u)
         done = 0
         for target in (1, 2, 7, 150):      # odd counts end in the swapped layout
             p.step(target - done)
