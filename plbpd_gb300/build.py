@@ -21,10 +21,10 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libplb_gb300.so")
-SOURCES = ["capi.cu", "kernels_ref.cu", "kernels_native.cu", "kernels_trt.cu", "kernels_h2_q9.cu", "kernels_h2_q19.cu",
+SOURCES = ["capi.cu", "kernels_ref.cu", "kernels_ref_cluster.cu", "kernels_native.cu", "kernels_trt.cu", "kernels_h2_q9.cu", "kernels_h2_q19.cu",
            "kernels_h2_q27.cu", "kernels_pair32_q9.cu", "kernels_pair32_q19.cu",
            "kernels_pair32_q27.cu", "kernels_util.cu", "kernels_static.cu", "facade.cpp", "server.cpp"]
-HEADERS = ["lattice.cuh", "tail_exact.h", "engine.h", "native_impl.cuh", "admission.h"]
+HEADERS = ["lattice.cuh", "tail_exact.h", "engine.h", "native_impl.cuh", "ref_ops.cuh", "admission.h"]
 FACADE_HEADERS = ["Boundary.hpp", "CalcMoments.hpp", "Collision.hpp", "CollisionSRT.hpp", "CollisionTRT.hpp", "Domain.hpp",
                   "EqlbDist.hpp", "Field.hpp", "Flow.hpp", "LBDynamics.hpp", "LBModel.hpp", "PLBPD.hpp", "SimData.hpp",
                   "Streaming.hpp"]

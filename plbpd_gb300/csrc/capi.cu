@@ -625,12 +625,40 @@ int run_chunk(plb_solve* s) {
     return PLB_OK;
 }
 
+// A REFERENCE march of a small D2Q9 domain runs in one cluster launch with
+// its state in distributed shared memory (kernels_ref_cluster.cu), unless
+// PLB_REF_CLUSTER=0.  D2Q9 moves in the x-z plane only; a north/south no-slip
+// face would make the whole plane a wall and keeps the three-launch path.
+bool ref_cluster_eligible(const plb_solve* s, int* C, int* R) {
+    const char* e = std::getenv("PLB_REF_CLUSTER");
+    if (e && std::strcmp(e, "0") == 0) return false;
+    if (s->q != 9 || s->g.ny != 1 || (s->fp.noslip_mask & 0x0c)) return false;
+    return ref_cluster_shape(s->g.nx, s->g.nz, C, R) != 0;
+}
+
+int ref_march_in_cluster(plb_solve* s, int C, int R, int64_t n) {
+    RefNoslipPlan plan{};
+    plan.ngroups = s->ngroups;
+    for (int i = 0; i < s->ngroups; ++i) {
+        plan.len[i] = s->group_len[i];
+        for (int j = 0; j < s->group_len[i]; ++j) plan.faces[i][j] = s->groups[i][j];
+    }
+    PLB_KERNEL(ref_march_cluster(s->karith, C, R, s->g, s->cp, s->fp, plan, (float*)s->f[0], (float*)s->f[1],
+                                 s->rho, s->u, s->cur, (long long)n, s->fields_valid, true, s->stream));
+    if (n & 1) s->cur = 1 - s->cur;
+    s->post = false;
+    s->fields_valid = false;
+    return PLB_OK;
+}
+
 int march(plb_solve* s, int64_t n) {
     if (n < 0) return fail(PLB_EINVAL, "negative step count");
     if (n == 0) return PLB_OK;
     const int64_t G = s->graph_steps;
     if (!s->native) {
         PLB_TRY(check_noslip_velocities(s));
+        int C = 0, R = 0;
+        if (ref_cluster_eligible(s, &C, &R)) return ref_march_in_cluster(s, C, R, n);
         // the first step reads the fields when they are the caller's; the
         // last writes every node back so the other buffer equals plbpd's ntmp
         int64_t done = 0;

@@ -63,6 +63,28 @@ int ref_noslip(int q, const Geo& g, const FaceParams& fp, const int* face_list, 
                float* n, const float* rho, cudaStream_t st);
 // East/west then north/south halo copies, as one launch.
 int ref_periodic(int q, const Geo& g, const FaceParams& fp, float* n, cudaStream_t st);
+
+// ---- REFERENCE semantics, whole marches in one launch (kernels_ref_cluster.cu)
+// The no-slip faces in launch groups, in plbpd's order (faces of a group
+// touch disjoint slots).
+struct RefNoslipPlan {
+    int ngroups;
+    int faces[6][2];
+    int len[6];
+};
+constexpr int kRefClusterMax = 16;        // CTAs of a cluster (above 8: non-portable size)
+constexpr int kRefClusterThreads = 1024;  // threads of a CTA
+// Cluster shape (CTAs, interior rows a CTA) for a D2Q9 domain of nx x nz
+// nodes held in distributed shared memory; 0 when it does not fit.
+int ref_cluster_shape(int nx, int nz, int* C, int* R);
+// n steps of plbpd's march on a D2Q9 domain (ny = 1, no north/south no-slip
+// face) in one launch per 2^20 steps: the first step takes rho/u from the
+// fields when `first`, the last writes every node back when `wb_last`, as
+// ref_fused_step does.  b0/b1 are the two population buffers, cur0 the one
+// holding n.  Returns a cudaError_t.
+int ref_march_cluster(int arith, int C, int R, const Geo& g, const CollideParams& cp, const FaceParams& fp,
+                      const RefNoslipPlan& plan, float* b0, float* b1, float* rho, const float* u, int cur0,
+                      long long nsteps, bool first, bool wb_last, cudaStream_t st);
 // Unfused operators.
 int ref_collide(int q, int arith, const Geo& g, const CollideParams& cp, float* n,
                 const float* rho, const float* u, cudaStream_t st);

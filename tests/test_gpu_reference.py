@@ -76,9 +76,13 @@ def test_sourcemap_matches_reference(case):
         assert_bitexact(s.get(1), ref["ntmp"], "source map ntmp")
 
 
-def test_channel_10000_steps_match_reference_digest(golden):
+@pytest.mark.parametrize("cluster", ["1", "0"])
+def test_channel_10000_steps_match_reference_digest(golden, monkeypatch, cluster):
     """The 128 x 64 D2Q9 channel, 10,000 steps in one march: every byte of n,
-    ntmp, rho and u equals the reference's."""
+    ntmp, rho and u equals the reference's -- with the march in one cluster
+    launch (state in distributed shared memory) and with three launches a
+    step (PLB_REF_CLUSTER=0)."""
+    monkeypatch.setenv("PLB_REF_CLUSTER", cluster)
     with gpu_solve(CHANNEL) as s:
         s.initialize()
         s.step(10000)
@@ -147,3 +151,27 @@ def test_conservation_matches_oracle():
         s.initialize()
         s.step(11)
         np.testing.assert_allclose(s.conservation(), p.conservation(), rtol=1e-12, atol=1e-13)
+
+
+@pytest.mark.parametrize("case", ["d2q9_channel"])
+@pytest.mark.parametrize("split", [(1,), (2, 3, 1), (7, 250, 9)])
+def test_cluster_march_equals_three_launch_path(case, split, monkeypatch):
+    """D2Q9 marches of various lengths (odd and even, first and last steps,
+    caller-set fields between marches) are identical with and without the
+    one-launch cluster path."""
+    from plbpd_gb300 import capi
+    cfg = CASES[case]
+    out = {}
+    for cluster in ("1", "0"):
+        monkeypatch.setenv("PLB_REF_CLUSTER", cluster)
+        with gpu_solve(cfg) as s:
+            s.initialize()
+            for i, n in enumerate(split):
+                s.step(n)
+                if i == 0:
+                    rho = s.get(capi.FIELD_RHO)
+                    rho[2:-2, 1, 2:-2, 0] *= np.float32(1.001)
+                    s.set(capi.FIELD_RHO, rho)
+            out[cluster] = [s.get(w) for _, w in FIELDS]
+    for (k, _), a, b in zip(FIELDS, out["1"], out["0"]):
+        assert_bitexact(a, b, f"{case} {split} {k}")
