@@ -1035,10 +1035,15 @@ size_t plb_field_len(const plb_solve* s, int32_t which) {
     }
 }
 
-int plb_get_field(plb_solve* s, int32_t which, float* out) {
-    if (!s || !out) return fail(PLB_EINVAL, "null argument");
-    if (which < PLB_FIELD_N || which > PLB_FIELD_U) return fail(PLB_EINVAL, "invalid field id");
-    PLB_TRY(set_device(s));
+}  // extern "C"
+
+namespace {
+// Enqueues a field read on the solve's stream (plb_get_field without the
+// wait).  `gathered`: a NATIVE state's moments are already in the rho/u
+// fields (a read of the other moment field came first).  `slot`: element
+// offset of the field in the staging buffer, which must hold
+// `staging_comps` components a cell.
+int enqueue_get_field(plb_solve* s, int32_t which, float* out, bool gathered, size_t slot, int staging_comps) {
     const size_t len = plb_field_len(s, which);
     int n_buf = s->cur;   // buffer that holds n for FIELD_N
     void* tmp = nullptr;   // AA: transient natural copy of a swapped buffer
@@ -1054,20 +1059,20 @@ int plb_get_field(plb_solve* s, int32_t which, float* out) {
                     cudaFreeAsync(tmp, s->stream);
                     return fail(PLB_ECUDA, std::string("nat_aa_gather: ") + cudaGetErrorString((cudaError_t)e));
                 }
-            } else if (which != PLB_FIELD_N) {
+            } else if (!gathered) {
                 PLB_KERNEL(nat_aa_gather(s->q, s->storage, s->has_mask, s->swapped, s->g, s->np, s->f[0], nullptr,
                                          s->rho, s->u, s->types, s->stream));
             }
         } else if (s->post) {
-            PLB_TRY(nat_gather_to_other(s));
+            if (!gathered || which == PLB_FIELD_N) PLB_TRY(nat_gather_to_other(s));
             n_buf = 1 - s->cur;
         }
     } else if (which == PLB_FIELD_RHO || which == PLB_FIELD_U) {
         PLB_TRY(ref_materialize_fields(s));
     }
     float* direct = device_view(out);
-    if (!direct) PLB_TRY(ensure_staging(s, (int)(len / ((size_t)(s->p.nx + 2) * (s->p.ny + 2) * (s->p.nz + 2)))));
-    float* aos = direct ? direct : s->staging;
+    if (!direct) PLB_TRY(ensure_staging(s, staging_comps));
+    float* aos = direct ? direct : s->staging + slot;
     const float* wk = s->consts + s->q;
     if (which == PLB_FIELD_N || which == PLB_FIELD_NTMP) {
         const void* src = tmp ? tmp : s->f[which == PLB_FIELD_N ? n_buf : 1 - s->cur];
@@ -1078,7 +1083,29 @@ int plb_get_field(plb_solve* s, int32_t which, float* out) {
         PLB_KERNEL(util_export(0, which == PLB_FIELD_RHO ? 1 : 3, s->g, which == PLB_FIELD_RHO ? s->rho : s->u,
                                nullptr, aos, s->stream));
     }
-    if (!direct) PLB_CUDA(cudaMemcpyAsync(out, s->staging, len * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    if (!direct) PLB_CUDA(cudaMemcpyAsync(out, aos, len * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    return PLB_OK;
+}
+}  // namespace
+
+int plb::read_moments(plb_solve* s, float* rho, float* u) {
+    if (!s || !rho || !u) return fail(PLB_EINVAL, "null argument");
+    PLB_TRY(set_device(s));
+    const size_t cells = plb_field_len(s, PLB_FIELD_RHO);
+    PLB_TRY(enqueue_get_field(s, PLB_FIELD_RHO, rho, false, 0, 4));
+    PLB_TRY(enqueue_get_field(s, PLB_FIELD_U, u, true, cells, 4));
+    return sync(s);
+}
+
+extern "C" {
+
+int plb_get_field(plb_solve* s, int32_t which, float* out) {
+    if (!s || !out) return fail(PLB_EINVAL, "null argument");
+    if (which < PLB_FIELD_N || which > PLB_FIELD_U) return fail(PLB_EINVAL, "invalid field id");
+    PLB_TRY(set_device(s));
+    const size_t len = plb_field_len(s, which);
+    const int comps = (int)(len / ((size_t)(s->p.nx + 2) * (s->p.ny + 2) * (s->p.nz + 2)));
+    PLB_TRY(enqueue_get_field(s, which, out, false, 0, comps));
     return sync(s);
 }
 

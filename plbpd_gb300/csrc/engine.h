@@ -24,6 +24,9 @@ int check_params(const plb_params* p);
 // `priority` (after the old stream's work); the solve server ranks its lanes.
 int set_solve_priority(plb_solve* s, int priority);
 int set_batch_priority(plb_batch* b, int priority);
+// rho and u of a solve in plbpd's layout (host memory), with one gather and
+// one wait for both (the solve server's retirement).
+int read_moments(plb_solve* s, float* rho, float* u);
 
 // Boundary description handed to the REFERENCE-semantics kernels.  Faces are
 // numbered east, west, north, south, up, down (plbpd's src/Boundary.cpp:17-18).

@@ -26,6 +26,7 @@
 #include <cmath>
 #include <chrono>
 #include <condition_variable>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <deque>
@@ -48,6 +49,7 @@ void record_error(const std::string& msg);   // capi.cu: the plb_last_error() sl
 int check_params(const plb_params* p);       // capi.cu: plb_solve_create's validation
 int set_solve_priority(plb_solve* s, int priority);   // capi.cu: move onto a stream of that priority
 int set_batch_priority(plb_batch* b, int priority);
+int read_moments(plb_solve* s, float* rho, float* u);   // capi.cu: rho and u with one wait
 }
 
 namespace {
@@ -150,8 +152,16 @@ struct plb_server {
     std::unordered_map<int64_t, std::unique_ptr<Req>> reqs;
     int64_t next_id = 1;
     // scheduler thread only
+    // seconds the scheduler spent creating solves, collecting finished ones,
+    // rebuilding batches and launching ticks, and sleeping with every lane
+    // busy (PLB_SERVER_STATS=1 prints them when the server stops)
+    double t_create = 0, t_retire = 0, t_rebuild = 0, t_launch = 0, t_idle = 0;
+    int64_t n_rebuild = 0, n_ticks = 0;
     std::map<ClassKey, std::unique_ptr<Lane>> batch_lanes;
     std::vector<std::unique_ptr<Lane>> solo_lanes;
+    // retired solves whose streams may still be busy: destroyed once idle,
+    // so retirement never waits for a destruction
+    std::vector<plb_solve*> graveyard;
     int prio_least = 0, prio_greatest = 0;   // cudaDeviceGetStreamPriorityRange
 
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
@@ -194,12 +204,25 @@ void retire(plb_server* srv, Req* r) {
     std::string err;
     r->rho.resize(plb_field_len(r->s, PLB_FIELD_RHO));
     r->u.resize(plb_field_len(r->s, PLB_FIELD_U));
-    if (plb_get_field(r->s, PLB_FIELD_RHO, r->rho.data()) != PLB_OK ||
-        plb_get_field(r->s, PLB_FIELD_U, r->u.data()) != PLB_OK)
-        err = plb_last_error();
-    plb_solve_destroy(r->s);
+    if (plb::read_moments(r->s, r->rho.data(), r->u.data()) != PLB_OK) err = plb_last_error();
+    srv->graveyard.push_back(r->s);
     r->s = nullptr;
     finish(srv, r, err.empty() ? PLB_REQ_DONE : PLB_REQ_FAILED, err);
+}
+
+// Destroys the retired solves whose streams have no work left (all of them
+// when `all`).
+void bury(plb_server* srv, bool all) {
+    for (size_t i = 0; i < srv->graveyard.size();) {
+        plb_solve* s = srv->graveyard[i];
+        if (all || cudaStreamQuery((cudaStream_t)plb_stream_handle(s)) != cudaErrorNotReady) {
+            plb_solve_destroy(s);
+            srv->graveyard[i] = srv->graveyard.back();
+            srv->graveyard.pop_back();
+        } else {
+            ++i;
+        }
+    }
 }
 
 // A running request cancelled by its client: its solve is destroyed and
@@ -252,6 +275,8 @@ void launch_tick(plb_server* srv, Lane& L) {
         stream = plb_stream_handle(L.members[0]->s);
     } else {
         if (L.dirty) {
+            const auto tr = Clock::now();
+            ++srv->n_rebuild;
             if (L.batch) plb_batch_destroy(L.batch);
             L.batch = nullptr;
             std::vector<plb_solve*> ss;
@@ -261,6 +286,7 @@ void launch_tick(plb_server* srv, Lane& L) {
             if (plb::set_batch_priority(L.batch, srv->prio_greatest) != PLB_OK)
                 return fail_lane(srv, L, plb_last_error());
             L.dirty = false;
+            srv->t_rebuild += std::chrono::duration<double>(Clock::now() - tr).count();
         }
         if (plb_batch_step_async(L.batch, t) != PLB_OK) return fail_lane(srv, L, plb_last_error());
         stream = plb_batch_stream_handle(L.batch);
@@ -349,7 +375,9 @@ void scheduler(plb_server* srv) {
             waiting = srv->pending.size();
         }
         for (Req* r : admitted) {
+            const auto tc = Clock::now();
             const std::string e = start_solve(r);
+            srv->t_create += std::chrono::duration<double>(Clock::now() - tc).count();
             if (!e.empty()) {
                 finish(srv, r, PLB_REQ_FAILED, e);
                 continue;
@@ -368,6 +396,15 @@ void scheduler(plb_server* srv) {
                 L->members.push_back(r);
                 srv->solo_lanes.push_back(std::move(L));
             } else {
+                // a batch member's own work (its read-back at retirement)
+                // runs at the batch lanes' priority, between their kernels
+                if (plb::set_solve_priority(r->s, srv->prio_greatest) != PLB_OK) {
+                    const std::string e2 = plb_last_error();
+                    plb_solve_destroy(r->s);
+                    r->s = nullptr;
+                    finish(srv, r, PLB_REQ_FAILED, e2);
+                    continue;
+                }
                 auto& L = srv->batch_lanes[ClassKey(r->p.q, r->p.storage, r->p.arith, r->p.collision)];
                 if (!L) L = std::make_unique<Lane>();
                 L->joining.push_back(r);
@@ -376,7 +413,12 @@ void scheduler(plb_server* srv) {
         // 2. collect ended ticks, 3. start the next ones
         bool progressed = !admitted.empty();
         auto service = [&](Lane& L) {
-            if (L.inflight && !collect_tick(srv, L)) return;
+            if (L.inflight) {
+                const auto tr = Clock::now();
+                const bool ended = collect_tick(srv, L);
+                srv->t_retire += std::chrono::duration<double>(Clock::now() - tr).count();
+                if (!ended) return;
+            }
             if (!L.joining.empty()) {
                 for (Req* r : L.joining) {
                     if (r->cancel) drop_cancelled(srv, r);
@@ -390,11 +432,15 @@ void scheduler(plb_server* srv) {
                 L.batch = nullptr;
                 return;
             }
+            const auto tl = Clock::now();
             launch_tick(srv, L);
+            ++srv->n_ticks;
+            srv->t_launch += std::chrono::duration<double>(Clock::now() - tl).count();
             progressed = true;
         };
         for (auto& kv : srv->batch_lanes) service(*kv.second);
         for (auto& L : srv->solo_lanes) service(*L);
+        bury(srv, false);
         for (size_t i = 0; i < srv->solo_lanes.size();) {
             Lane& L = *srv->solo_lanes[i];
             if (L.members.empty() && !L.inflight) {
@@ -406,9 +452,11 @@ void scheduler(plb_server* srv) {
         }
         if (!progressed) {
             // every lane is mid-tick: sleep briefly, or until a new request arrives
+            const auto ti = Clock::now();
             std::unique_lock<std::mutex> lk(srv->mu);
             srv->work_cv.wait_for(lk, std::chrono::microseconds(200),
                                   [&] { return srv->stop || srv->pending.size() > waiting; });
+            srv->t_idle += std::chrono::duration<double>(Clock::now() - ti).count();
         }
     }
     // stop: wait for the ticks in flight, then drop everything
@@ -424,6 +472,7 @@ void scheduler(plb_server* srv) {
     for (auto& L : srv->solo_lanes) drop(*L);
     srv->batch_lanes.clear();
     srv->solo_lanes.clear();
+    bury(srv, true);
 }
 
 }  // namespace
@@ -583,6 +632,13 @@ int plb_server_stop(plb_server* srv) {
         srv->work_cv.notify_all();
     }
     if (srv->th.joinable()) srv->th.join();
+    const char* st = std::getenv("PLB_SERVER_STATS");
+    if (st && std::strcmp(st, "1") == 0)
+        std::fprintf(stderr,
+                     "plb_server: create %.3f s, collect/retire %.3f s, batch rebuilds %.3f s (%lld), "
+                     "tick launches %.3f s (%lld), idle %.3f s\n",
+                     srv->t_create, srv->t_retire, srv->t_rebuild, (long long)srv->n_rebuild, srv->t_launch,
+                     (long long)srv->n_ticks, srv->t_idle);
     delete srv;
     return PLB_OK;
 }
