@@ -233,6 +233,11 @@ int plb_tune_variant(const plb_solve* s, int32_t* variant);
  * points (initialize, set/get field, set mask, conservation) still apply
  * between batch calls, and each member's stream waits for the batch's work
  * of the last call, so they see its result without plb_batch_synchronize.
+ * A step is one launch, the step loop replayed as CUDA-graph chunks; with
+ * PLB_BATCH_MULTI=1 a call's steps run as one cooperative launch with a
+ * grid barrier between steps instead (its loads bypass L1, which costs a few
+ * per cent), and a barrier whose wait runs out ends the launch and the next
+ * plb_batch_synchronize returns PLB_ETIMEOUT.
  * A batch keeps the kernel chosen at creation: after a member's lattice
  * arithmetic or collision changes (plb_set_collision) or it gains a moving
  * wall, plb_batch_step refuses with PLB_ESTATE; create a new batch.
@@ -243,6 +248,13 @@ int plb_batch_step(plb_batch* b, int64_t nsteps);
 int plb_batch_step_async(plb_batch* b, int64_t nsteps);
 int plb_batch_synchronize(plb_batch* b);
 int plb_batch_destroy(plb_batch* b);
+/* Fault injection for tests of the timeout path (PLB_BATCH_MULTI=1): the
+ * next plb_batch_step's multi-step launch starts its grid barrier in a state
+ * no arrival completes, so the first barrier's bounded wait runs out (about
+ * a second), the kernel ends, and plb_batch_synchronize returns
+ * PLB_ETIMEOUT.  The members' state is then undefined (some steps ran, some
+ * did not).  No counterpart in plbpd. */
+int plb_batch_fault_barrier(plb_batch* b);
 /* Cells of all member domains. */
 int64_t plb_batch_cells(const plb_batch* b);
 /* The batch's CUDA stream (a cudaStream_t). */

@@ -83,6 +83,7 @@ _SIGS = [
     ("plb_batch_synchronize", C.c_int, [C.c_void_p]),
     ("plb_batch_destroy", C.c_int, [C.c_void_p]),
     ("plb_batch_cells", C.c_int64, [C.c_void_p]),
+    ("plb_batch_fault_barrier", C.c_int, [C.c_void_p]),
     ("plb_batch_stream_handle", C.c_void_p, [C.c_void_p]),
     ("plb_solve_bytes", C.c_int64, [C.POINTER(Params)]),
     ("plb_server_start", C.c_int, [C.c_int32, C.c_int64, C.c_int32, C.POINTER(C.c_void_p)]),
@@ -305,6 +306,7 @@ class Batch:
     def step_async(self, n: int = 1) -> None: check(lib().plb_batch_step_async(self.h, int(n)))
     def synchronize(self) -> None: check(lib().plb_batch_synchronize(self.h))
     def cells(self) -> int: return int(lib().plb_batch_cells(self.h))
+    def fault_barrier(self) -> None: check(lib().plb_batch_fault_barrier(self.h))
 
     def close(self) -> None:
         if getattr(self, "h", None):

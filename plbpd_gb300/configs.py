@@ -19,7 +19,8 @@ c3  D3Q27 384^3 duct (walls on y and z, periodic x) with 15 % random spheres,
     500 steps; L2 of rho and u against FP64 after --c3-accuracy-steps steps
     (an FP64 run of all 5,000 steps takes minutes).
 c4  512 D3Q19 domains (edges log-uniform in [16, 96], porosity 0.7-0.9),
-    1,000 steps: one batch against per-domain solves, FP32 and FP16.
+    1,000 steps: one batch (a launch a step, graph-replayed; and all steps in
+    one cooperative launch) against per-domain solves, FP32 and FP16.
 c5  the served stream: a prefix of the mixed trace and a trace of small
     requests, each served and run as plain solves one after another, with
     accuracy against FP64 runs (plbpd_gb300.serve_bench).
@@ -31,6 +32,7 @@ from __future__ import annotations
 import argparse
 import hashlib
 import json
+import os
 import time
 
 import numpy as np
@@ -188,6 +190,21 @@ def config4(steps: int = 1000, domains: int = 512, storages=("fp32", "fp16"), se
             t0 = time.perf_counter()
             b.step(steps)
             tb = time.perf_counter() - t0
+        # the same steps as one cooperative launch with grid barriers
+        prev = os.environ.get("PLB_BATCH_MULTI")
+        os.environ["PLB_BATCH_MULTI"] = "1"
+        try:
+            with capi.Batch(solves) as b:
+                b.step(2)
+                b.synchronize()
+                t0 = time.perf_counter()
+                b.step(steps)
+                tm = time.perf_counter() - t0
+        finally:
+            if prev is None:
+                del os.environ["PLB_BATCH_MULTI"]
+            else:
+                os.environ["PLB_BATCH_MULTI"] = prev
         for s in solves:
             s.synchronize()
         t0 = time.perf_counter()
@@ -199,6 +216,7 @@ def config4(steps: int = 1000, domains: int = 512, storages=("fp32", "fp16"), se
         for s in solves:
             s.close()
         out[st_name] = {"cells": int(cells), "batch_mlups": _mlups(cells, steps, tb),
+                        "batch_one_launch_mlups": _mlups(cells, steps, tm),
                         "per_domain_mlups": _mlups(cells, steps, tp), "speedup": round(tp / tb, 3),
                         "setup_seconds": round(setup, 1)}
     return out

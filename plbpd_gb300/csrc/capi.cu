@@ -1204,6 +1204,12 @@ struct plb_batch {
     cudaEvent_t done = nullptr;   // recorded after each batch call's work
     std::vector<cudaEvent_t> member_ev;   // one per member: its own work so far
     std::vector<BatchDomain> h_doms;
+    // multi-step launches (PLB_BATCH_MULTI=1: one cooperative launch runs a
+    // call's steps, a grid barrier between them)
+    bool multi = false;
+    BatchSync* d_sync = nullptr;
+    int* err_host = nullptr;   // the barrier's error word after the last launch (page-locked)
+    bool fault_next = false;   // plb_batch_fault_barrier: the next launch's first barrier cannot complete
 };
 
 namespace {
@@ -1214,12 +1220,14 @@ void batch_release(plb_batch* b) {
     if (b->done) cudaEventDestroy(b->done);
     for (cudaEvent_t e : b->member_ev)
         if (e) cudaEventDestroy(e);
+    if (b->d_sync) cudaFreeAsync(b->d_sync, b->stream);
     if (b->d_doms) cudaFreeAsync(b->d_doms, b->stream);
     if (b->d_tiles) cudaFreeAsync(b->d_tiles, b->stream);
     if (b->stream) {
         cudaStreamSynchronize(b->stream);
         cudaStreamDestroy(b->stream);
     }
+    if (b->err_host) cudaFreeHost(b->err_host);
     delete b;
 }
 
@@ -1362,9 +1370,20 @@ int plb_batch_create(int32_t n, plb_solve* const* solves, plb_batch** out) {
     b->blocks = (dev_sms > 0 ? dev_sms : 1) * (per_sm > 0 ? per_sm : 1);
     // stream-ordered, like a solve's memory
     if (cudaMallocAsync(&b->d_doms, n * sizeof(BatchDomain), b->stream) != cudaSuccess ||
-        cudaMallocAsync(&b->d_tiles, tiles.size() * sizeof(int4), b->stream) != cudaSuccess) {
+        cudaMallocAsync(&b->d_tiles, tiles.size() * sizeof(int4), b->stream) != cudaSuccess ||
+        cudaMallocAsync(&b->d_sync, sizeof(BatchSync), b->stream) != cudaSuccess) {
         batch_release(b);
         return fail(PLB_ENOMEM, "batch tables");
+    }
+    if (cudaHostAlloc(&b->err_host, sizeof(int), cudaHostAllocDefault) != cudaSuccess) {
+        b->err_host = nullptr;
+        batch_release(b);
+        return fail(PLB_ENOMEM, "batch error word");
+    }
+    *b->err_host = 0;
+    {
+        const char* e = std::getenv("PLB_BATCH_MULTI");
+        b->multi = e && std::strcmp(e, "1") == 0;
     }
     if (cudaMemcpyAsync(b->d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, b->stream) !=
             cudaSuccess ||
@@ -1393,6 +1412,25 @@ int plb_batch_step_async(plb_batch* b, int64_t nsteps) {
     int64_t i = 0;
     const int64_t todo = nsteps - done;
     const int64_t G = b->graph_steps;
+    // multi-step launches, chunks of at most 2^16 steps; a configuration
+    // the cooperative launch refuses (too many blocks for co-residency)
+    // falls back to one launch a step
+    while (b->multi && i < todo) {
+        const int n = (int)(todo - i < (1 << 16) ? todo - i : (1 << 16));
+        BatchSync init{b->fault_next ? 0x7fffffffu : 0u, 0u, 0};
+        b->fault_next = false;
+        PLB_CUDA(cudaMemcpyAsync(b->d_sync, &init, sizeof(init), cudaMemcpyHostToDevice, b->stream));
+        const int rc = nat_batch_step_multi(b->q, b->storage, b->arith, b->moving, b->pairs, b->d_doms, b->d_tiles,
+                                            b->ntiles, (int)(i & 1), n, b->blocks, b->d_sync, b->stream);
+        if (rc == (int)cudaErrorCooperativeLaunchTooLarge || rc == (int)cudaErrorInvalidConfiguration) {
+            cudaGetLastError();
+            b->multi = false;
+            break;
+        }
+        if (rc != 0) return fail(PLB_ECUDA, std::string("nat_batch_step_multi: ") + cudaGetErrorString((cudaError_t)rc));
+        PLB_CUDA(cudaMemcpyAsync(b->err_host, &b->d_sync->error, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+        i += n;
+    }
     while (G > 0 && todo - i >= G) {
         if (!b->graph) PLB_TRY(batch_capture(b));
         PLB_CUDA(cudaGraphLaunch(b->graph, b->stream));
@@ -1413,6 +1451,17 @@ int plb_batch_step_async(plb_batch* b, int64_t nsteps) {
 int plb_batch_synchronize(plb_batch* b) {
     if (!b) return fail(PLB_EINVAL, "batch is null");
     PLB_CUDA(cudaStreamSynchronize(b->stream));
+    if (*b->err_host) {
+        *b->err_host = 0;
+        return fail(PLB_ETIMEOUT, "a grid barrier of the multi-step batch kernel waited too long; the steps of "
+                                  "that launch did not all run");
+    }
+    return PLB_OK;
+}
+
+int plb_batch_fault_barrier(plb_batch* b) {
+    if (!b) return fail(PLB_EINVAL, "batch is null");
+    b->fault_next = true;
     return PLB_OK;
 }
 

@@ -174,6 +174,19 @@ int nat_batch_step(int q, int storage, int arith, bool moving, bool pairs, const
 // Resident blocks per SM of the batch kernel (for sizing the grid).
 int nat_batch_blocks_per_sm(int q, int storage, int arith, bool moving, bool pairs);
 constexpr int kBatchTile = 128;
+// The multi-step batch kernel's grid barrier (device memory; count and error
+// start at 0; error becomes 1 when a barrier's wait ran out).
+struct BatchSync {
+    unsigned int count;
+    unsigned int gen;
+    int error;
+};
+// nsteps steps of the batch in one cooperative launch (at most `blocks`
+// blocks, no more than can be resident), a grid barrier between steps; the
+// parities alternate from `parity` as with nsteps calls of nat_batch_step.
+int nat_batch_step_multi(int q, int storage, int arith, bool moving, bool pairs, const BatchDomain* doms,
+                         const int4* tiles, int ntiles, int parity, int nsteps, int blocks, BatchSync* bs,
+                         cudaStream_t st);
 
 // The TRT instantiations behind the functions above (kernels_trt.cu).
 int nat_fused_step_trt(int q, int storage, bool has_mask, const Geo& g, const CollideParams& cp,
@@ -187,6 +200,9 @@ int nat_aa_step_trt(int kind, int q, int storage, bool has_mask, const Geo& g, c
 int nat_batch_blocks_per_sm_trt(int q, int storage, bool moving, bool pairs);
 int nat_batch_step_trt(int q, int storage, bool moving, bool pairs, const BatchDomain* doms, const int4* tiles,
                        int ntiles, int parity, int blocks, cudaStream_t st);
+int nat_batch_step_multi_trt(int q, int storage, bool moving, bool pairs, const BatchDomain* doms,
+                             const int4* tiles, int ntiles, int parity, int nsteps, int blocks, BatchSync* bs,
+                             cudaStream_t st);
 
 // ---- shared (kernels_util.cu) ----------------------------------------------
 // Every node of the box (halo included): rho0, u0, n = feq, ntmp = 0.

@@ -191,6 +191,15 @@ int nat_batch_step(int q, int storage, int arith, bool moving, bool pairs, const
     return batch_step<false>(q, storage, arith, moving, pairs, doms, tiles, ntiles, parity, blocks, st);
 }
 
+int nat_batch_step_multi(int q, int storage, int arith, bool moving, bool pairs, const BatchDomain* doms,
+                         const int4* tiles, int ntiles, int parity, int nsteps, int blocks, BatchSync* bs,
+                         cudaStream_t st) {
+    if (arith == kArithTRT)
+        return nat_batch_step_multi_trt(q, storage, moving, pairs, doms, tiles, ntiles, parity, nsteps, blocks, bs, st);
+    return batch_step_multi<false>(q, storage, arith, moving, pairs, doms, tiles, ntiles, parity, nsteps, blocks, bs,
+                                   st);
+}
+
 int nat_reset_fields(const Geo& g, const NativeParams& np, const uint8_t* types, float* rho, float* u,
                      cudaStream_t st) {
     nat_reset_fields_k<<<cell_grid(g), kBlockX, 0, st>>>(g, np, types, rho, u);

@@ -36,4 +36,11 @@ int nat_batch_step_trt(int q, int storage, bool moving, bool pairs, const BatchD
     return batch_step<true>(q, storage, kArithTRT, moving, pairs, doms, tiles, ntiles, parity, blocks, st);
 }
 
+int nat_batch_step_multi_trt(int q, int storage, bool moving, bool pairs, const BatchDomain* doms,
+                             const int4* tiles, int ntiles, int parity, int nsteps, int blocks, BatchSync* bs,
+                             cudaStream_t st) {
+    return batch_step_multi<true>(q, storage, kArithTRT, moving, pairs, doms, tiles, ntiles, parity, nsteps, blocks,
+                                  bs, st);
+}
+
 }  // namespace plb

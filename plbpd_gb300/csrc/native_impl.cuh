@@ -87,6 +87,17 @@ template <> struct Store<2> {
     __device__ static __forceinline__ void st(double* p, long long i, double v) { __stcs(p + i, v); }
 };
 
+// A population load: through the read-only path (the buffer is not written
+// while the kernel runs), or, CG, cached in L2 only -- the multi-step batch
+// kernel reads in one step what other SMs wrote in the previous one, which
+// an SM's L1 or read-only cache may still hold from two steps before.
+template <int ST, bool CG>
+__device__ __forceinline__ typename Store<ST>::R ld_pop(const typename Store<ST>::T* p, long long i) {
+    if constexpr (!CG) return Store<ST>::ld(p, i);
+    else if constexpr (ST == 1) return __half2float(__ldcg(p + i));
+    else return __ldcg(p + i);
+}
+
 // Neighbour index helper: element offsets of x-1, x, x+1 (and y, z) with the
 // periodic axes wrapped.  A fluid node never has a neighbour outside the box
 // along a walled axis, because the wall layer in between is solid, so kernels
@@ -653,29 +664,29 @@ __device__ __forceinline__ uint32_t links_of(const uint8_t t, const uint32_t* __
 // node too), so the streaming loads are unconditional; bounce-back directions
 // are then replaced by the node's own reversed slot.  `links` bit k is set
 // when x + c_k is solid, so the source x - c_k is solid when bit rev(k) is.
-template <int Q, int ST>
+template <int Q, int ST, bool CG = false>
 __device__ __forceinline__ void stream_loads(const typename Store<ST>::T* __restrict__ src, const Geo& g,
                                              const Nbr& nb, typename Store<ST>::R (&f)[Q]) {
 #pragma unroll
-    for (int k = 0; k < Q; ++k) f[k] = Store<ST>::ld(src, k * g.ks + nb.at<Q>(k, -1));
+    for (int k = 0; k < Q; ++k) f[k] = ld_pop<ST, CG>(src, k * g.ks + nb.at<Q>(k, -1));
 }
 
-template <int Q, int ST>
+template <int Q, int ST, bool CG = false>
 __device__ __forceinline__ void bounce_fixup(const typename Store<ST>::T* __restrict__ src, const Geo& g,
                                              uint32_t links, long long node, typename Store<ST>::R (&f)[Q]) {
     if (links) {
 #pragma unroll
         for (int k = 1; k < Q; ++k)
-            if ((links >> rev_of(k)) & 1u) f[k] = Store<ST>::ld(src, rev_of(k) * g.ks + node);
+            if ((links >> rev_of(k)) & 1u) f[k] = ld_pop<ST, CG>(src, rev_of(k) * g.ks + node);
     }
 }
 
-template <int Q, int ST, bool MASK>
+template <int Q, int ST, bool MASK, bool CG = false>
 __device__ __forceinline__ void gather_node(const typename Store<ST>::T* __restrict__ src, const Geo& g,
                                             uint32_t links, const Nbr& nb, long long node,
                                             typename Store<ST>::R (&f)[Q]) {
-    stream_loads<Q, ST>(src, g, nb, f);
-    if (MASK) bounce_fixup<Q, ST>(src, g, links, node, f);
+    stream_loads<Q, ST, CG>(src, g, nb, f);
+    if (MASK) bounce_fixup<Q, ST, CG>(src, g, links, node, f);
 }
 
 // ---------------------------------------------------------------------------
@@ -730,7 +741,7 @@ nat_fused_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::
 // The same two-node scheme serves FP32 and FP32-deviation storage (ST 0 and
 // 3: one aligned float2 a lane and direction), where it halves the
 // instructions a node takes and doubles the bytes a thread has in flight.
-template <int Q, bool MASK, bool MOVING, int ARITH, int FORM = 0, int ST = 1>
+template <int Q, bool MASK, bool MOVING, int ARITH, int FORM = 0, int ST = 1, bool CG = false>
 __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, const NativeParams& np,
                                         const typename Store<ST>::T* __restrict__ src,
                                         typename Store<ST>::T* __restrict__ dst, const uint8_t* __restrict__ types,
@@ -767,18 +778,23 @@ __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, c
         const long long row = (long long)k * g.ks + zo[1 - cz] + yo[1 - cy];
         float2 v = make_float2(0.0f, 0.0f);
         if (active) {
-            if constexpr (ST == 1) v = __half22float2(__ldg(reinterpret_cast<const __half2*>(src + row + x0)));
-            else v = __ldg(reinterpret_cast<const float2*>(src + row + x0));
+            if constexpr (ST == 1) {
+                const __half2* a = reinterpret_cast<const __half2*>(src + row + x0);
+                v = __half22float2(CG ? __ldcg(a) : __ldg(a));
+            } else {
+                const float2* a = reinterpret_cast<const float2*>(src + row + x0);
+                v = CG ? __ldcg(a) : __ldg(a);
+            }
         }
         if (cx == 0) {
             f[k] = v;
         } else if (cx > 0) {
             float prev = __shfl_up_sync(kFull, v.y, 1);
-            if (edge_lo) prev = (active && xm >= 0) ? Store<ST>::ld(src, row + xm) : 0.0f;
+            if (edge_lo) prev = (active && xm >= 0) ? ld_pop<ST, CG>(src, row + xm) : 0.0f;
             f[k] = make_float2(prev, v.x);
         } else {
             float next = __shfl_down_sync(kFull, v.x, 1);
-            if (edge_hi) next = (active && xp2 >= 0) ? Store<ST>::ld(src, row + xp2) : 0.0f;
+            if (edge_hi) next = (active && xp2 >= 0) ? ld_pop<ST, CG>(src, row + xp2) : 0.0f;
             f[k] = make_float2(v.y, next);
         }
     }
@@ -787,8 +803,8 @@ __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, c
 #pragma unroll
         for (int k = 1; k < Q; ++k) {
             const long long slot = (long long)rev_of(k) * g.ks + node0;
-            if ((L0 >> rev_of(k)) & 1u) f[k].x = Store<ST>::ld(src, slot);
-            if ((L1 >> rev_of(k)) & 1u) f[k].y = Store<ST>::ld(src, slot + 1);
+            if ((L0 >> rev_of(k)) & 1u) f[k].x = ld_pop<ST, CG>(src, slot);
+            if ((L1 >> rev_of(k)) & 1u) f[k].y = ld_pop<ST, CG>(src, slot + 1);
         }
     }
     float2 rho;
@@ -1086,9 +1102,11 @@ nat_gather_k(Geo g, NativeParams np, const typename Store<ST>::T* __restrict__ s
 // so each lane forms its own row offsets.  A task's kind is the same for the
 // whole warp.  FP16 pairs use the paired update (form 0), FP32 storages the
 // scalar update of each node (form 2), which serves every arithmetic.
-template <int Q, int ST, int ARITH, bool MOVING, bool PAIRS = false>
-__global__ void __launch_bounds__(kBatchTile)
-nat_batch_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks, int ntasks, int parity) {
+// The tasks of one step, walked by every resident warp (CG: L2-coherent
+// population loads, for the multi-step kernel).
+template <int Q, int ST, int ARITH, bool MOVING, bool PAIRS, bool CG>
+__device__ __forceinline__ void batch_tasks(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks,
+                                            int ntasks, int parity) {
     using T = typename Store<ST>::T;
     using R = typename Store<ST>::R;
     const int lane = threadIdx.x & 31;
@@ -1102,9 +1120,9 @@ nat_batch_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks
             const bool active = i < g.nx * g.ny;
             const int y = active ? (int)((unsigned)i / (unsigned)g.nx) : 0;
             const int x0 = active ? i - y * g.nx : 0;
-            h2_pair<Q, true, MOVING, ARITH, ST == 1 ? 0 : 2, ST>(g, D.cp, D.np, static_cast<const T*>(D.f[parity]),
-                                                                static_cast<T*>(D.f[parity ^ 1]), D.types, lane, x0,
-                                                                y, tk.y, active);
+            h2_pair<Q, true, MOVING, ARITH, ST == 1 ? 0 : 2, ST, CG>(g, D.cp, D.np, static_cast<const T*>(D.f[parity]),
+                                                                    static_cast<T*>(D.f[parity ^ 1]), D.types, lane,
+                                                                    x0, y, tk.y, active);
             continue;
         }
         // 32 consecutive nodes of the plane z (flattened y * nx + x), so short
@@ -1122,10 +1140,67 @@ nat_batch_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks
         T* dst = static_cast<T*>(D.f[parity ^ 1]);
         const Nbr nb(g, x, y, z);
         R f[Q];
-        gather_node<Q, ST, true>(src, g, L, nb, node, f);
+        gather_node<Q, ST, true, CG>(src, g, L, nb, node, f);
         R rho;
         update_node<Q, ST, ARITH>(f, rho, D.cp);
         store_node<Q, ST, true, MOVING>(dst, g, np, types, L, nb, node, rho, f);
+    }
+}
+
+template <int Q, int ST, int ARITH, bool MOVING, bool PAIRS = false>
+__global__ void __launch_bounds__(kBatchTile)
+nat_batch_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks, int ntasks, int parity) {
+    batch_tasks<Q, ST, ARITH, MOVING, PAIRS, false>(doms, tasks, ntasks, parity);
+}
+
+// ---------------------------------------------------------------------------
+// Multi-step batches: one launch runs n steps of the task list, the steps
+// separated by a grid-wide barrier.  The grid is what can be resident at once
+// (a cooperative launch), so every block reaches every barrier.  The wait at
+// a barrier is bounded: a block that polls more than kBatchBarrierPolls times
+// sets the error word and leaves, the others see the word and leave too, and
+// the host reports PLB_ETIMEOUT; a step's own work never takes that long.
+// Population loads bypass L1 (CG): a step reads what other SMs wrote in the
+// previous one.
+constexpr unsigned long long kBatchBarrierPolls = 1ull << 22;   // about 1-2 s with the back-off
+
+__device__ __forceinline__ bool batch_grid_sync(BatchSync* bs, unsigned nblocks) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        volatile unsigned int* vgen = &bs->gen;
+        volatile int* verr = &bs->error;
+        const unsigned int g0 = *vgen;   // read before arriving: it cannot change until this block arrives
+        __threadfence();                 // this block's stores before its arrival
+        if (atomicAdd(&bs->count, 1u) == nblocks - 1) {
+            atomicExch(&bs->count, 0u);
+            __threadfence();
+            atomicAdd(&bs->gen, 1u);
+        } else {
+            unsigned long long polls = 0;
+            while (*vgen == g0) {
+                if (*verr || ++polls > kBatchBarrierPolls) {
+                    atomicExch(&bs->error, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();                 // the other blocks' stores before this block's next loads
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+template <int Q, int ST, int ARITH, bool MOVING, bool PAIRS = false>
+__global__ void __launch_bounds__(kBatchTile)
+nat_batch_multi_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks, int ntasks, int parity,
+                  int nsteps, BatchSync* bs) {
+    for (int s = 0; s < nsteps; ++s) {
+        batch_tasks<Q, ST, ARITH, MOVING, PAIRS, true>(doms, tasks, ntasks, parity ^ (s & 1));
+        if (s + 1 < nsteps && !batch_grid_sync(bs, gridDim.x)) return;
     }
 }
 
@@ -1387,6 +1462,51 @@ int batch_step(int q, int storage, int arith, bool moving, bool pairs, const Bat
         };
         return q == 9 ? go(IC<9>{}) : q == 19 ? go(IC<19>{}) : q == 27 ? go(IC<27>{}) : (int)cudaErrorInvalidValue;
     });
+}
+
+// The multi-step kernel for a configuration (nullptr if none).
+template <bool TRT, bool MV>
+const void* batch_multi_kernel_for(int q, int storage, int arith, bool pairs) {
+    const void* k = nullptr;
+    with_storage_arith<TRT>(storage == 2 ? 0 : storage, arith, [&](auto stc, auto arc) {
+        constexpr int ST = decltype(stc)::value == 2 ? 0 : decltype(stc)::value, AR = decltype(arc)::value;
+        if (pairs)
+            k = q == 9 ? (const void*)nat_batch_multi_k<9, ST, AR, MV, true>
+              : q == 19 ? (const void*)nat_batch_multi_k<19, ST, AR, MV, true>
+              : q == 27 ? (const void*)nat_batch_multi_k<27, ST, AR, MV, true> : nullptr;
+        else
+            k = q == 9 ? (const void*)nat_batch_multi_k<9, ST, AR, MV>
+              : q == 19 ? (const void*)nat_batch_multi_k<19, ST, AR, MV>
+              : q == 27 ? (const void*)nat_batch_multi_k<27, ST, AR, MV> : nullptr;
+        return 0;
+    });
+    return k;
+}
+
+// nsteps steps in one cooperative launch of at most `blocks` blocks (no more
+// than are resident at once on the device); bs must hold count = 0 and
+// error = 0.
+template <bool TRT>
+int batch_step_multi(int q, int storage, int arith, bool moving, bool pairs, const BatchDomain* doms,
+                     const int4* tiles, int ntiles, int parity, int nsteps, int blocks, BatchSync* bs,
+                     cudaStream_t st) {
+    if (ntiles <= 0 || nsteps <= 0) return 0;
+    if (storage == 2) return (int)cudaErrorInvalidValue;
+    const void* k = moving ? batch_multi_kernel_for<TRT, true>(q, storage, arith, pairs)
+                           : batch_multi_kernel_for<TRT, false>(q, storage, arith, pairs);
+    if (!k) return (int)cudaErrorInvalidValue;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kBatchTile, 0);
+    if (e != cudaSuccess) return (int)e;
+    const int resident = sms * per_sm;
+    const int need = (ntiles + kBatchTile / 32 - 1) / (kBatchTile / 32);
+    if (blocks > resident) blocks = resident;
+    if (blocks > need) blocks = need;
+    if (blocks < 1) return (int)cudaErrorInvalidConfiguration;
+    void* args[] = {(void*)&doms, (void*)&tiles, (void*)&ntiles, (void*)&parity, (void*)&nsteps, (void*)&bs};
+    return (int)cudaLaunchCooperativeKernel(k, dim3((unsigned)blocks), dim3(kBatchTile), args, 0, st);
 }
 
 #define PLB_Q_DISPATCH(q, CALL) \

@@ -303,6 +303,11 @@ bool collect_tick(plb_server* srv, Lane& L) {
         fail_lane(srv, L, std::string("tick failed: ") + cudaGetErrorString(q));
         return true;
     }
+    // a batch tick's multi-step launch reports a grid barrier that timed out
+    if (!L.solo && L.batch && plb_batch_synchronize(L.batch) != PLB_OK) {
+        fail_lane(srv, L, plb_last_error());
+        return true;
+    }
     std::vector<Req*> keep;
     for (Req* r : L.members) {
         r->remaining -= L.inflight;

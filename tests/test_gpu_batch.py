@@ -34,11 +34,15 @@ def make_solves(capi, storage, seed=5, count=7, model="D3Q19", even_fp16=True):
     return out
 
 
+@pytest.mark.parametrize("multi", ["0", "1"])
 @pytest.mark.parametrize("storage_name", ["fp32", "fp16", "fp16_odd", "fp32dev"])
 @pytest.mark.parametrize("model", ["D3Q19", "D3Q27"])
-def test_batch_equals_each_domain_alone(storage_name, model):
+def test_batch_equals_each_domain_alone(storage_name, model, multi, monkeypatch):
     """Domains with even nx run as pair tasks, the others as one-node tasks,
-    in the same launch (fp16_odd: FP16 domains of both kinds)."""
+    in the same launch (fp16_odd: FP16 domains of both kinds); one launch a
+    step in graph chunks, or a call's steps in one cooperative launch with
+    grid barriers (PLB_BATCH_MULTI=1)."""
+    monkeypatch.setenv("PLB_BATCH_MULTI", multi)
     from plbpd_gb300 import capi
     storage = {"fp32": capi.STORAGE_FP32, "fp16": capi.STORAGE_FP16_DEV, "fp16_odd": capi.STORAGE_FP16_DEV,
                "fp32dev": capi.STORAGE_FP32_DEV}[storage_name]
@@ -116,3 +120,31 @@ def test_member_calls_follow_batch_without_synchronize():
     for a, g, c in zip(alone, got, cons):
         assert np.array_equal(a.get(capi.FIELD_U).view(np.uint32), g.view(np.uint32))
         np.testing.assert_array_equal(a.conservation(), c)
+
+
+def test_batch_barrier_timeout_is_reported(monkeypatch):
+    """A grid barrier of the multi-step kernel that cannot complete (fault
+    injection: its arrival count starts past the grid) ends the launch after
+    its bounded wait; plb_batch_synchronize reports PLB_ETIMEOUT and the
+    context stays usable: a fresh batch of the same domains then matches
+    the domains advanced alone."""
+    import time
+    from plbpd_gb300 import capi
+    monkeypatch.setenv("PLB_BATCH_MULTI", "1")
+    mix = make_solves(capi, capi.STORAGE_FP32, seed=21, count=3)
+    with capi.Batch(mix) as b:
+        b.step(2)
+        b.fault_barrier()
+        t0 = time.perf_counter()
+        with pytest.raises(capi.PlbError) as e:
+            b.step(5)
+        assert e.value.code == capi.ETIMEOUT
+        assert time.perf_counter() - t0 < 60.0
+    fresh = make_solves(capi, capi.STORAGE_FP32, seed=23, count=3)
+    alone = make_solves(capi, capi.STORAGE_FP32, seed=23, count=3)
+    with capi.Batch(fresh) as b:
+        b.step(9)
+    for s in alone:
+        s.step(9)
+    for a, m in zip(alone, fresh):
+        assert np.array_equal(a.get(capi.FIELD_U).view(np.uint32), m.get(capi.FIELD_U).view(np.uint32))
