@@ -18,9 +18,11 @@
 // to it (and to plbpd): the fused phase is ref_fused_step_k's body, the
 // no-slip phase ref_noslip_k's (with its serial order of in-plane pairs), the
 // periodic phase ref_periodic_k's east/west copy.  A step has one cluster
-// barrier after the pushes and one after each no-slip face group (the
-// hardware cluster barrier; no thread waits on a flag); the periodic copies
-// of a CTA's own rows end with a CTA barrier.
+// barrier after the pushes, and one after each no-slip face group unless
+// every no-slip access stays inside one CTA (up/down walls with two or more
+// rows a CTA: then a CTA barrier); the periodic copies of a CTA's own rows
+// end with a CTA barrier.  The barriers are the hardware's; no thread waits
+// on a flag.
 #include <cooperative_groups.h>
 
 #include "engine.h"
@@ -113,7 +115,8 @@ __device__ __forceinline__ void noslip_node(const Geo& g, const FaceParams& fp, 
 template <int ARITH>
 __global__ void __launch_bounds__(kRefClusterThreads)
 ref_march_cluster_k(Geo g, CollideParams cp, FaceParams fp, RefNoslipPlan plan, float* b0, float* b1,
-                    float* rho_g, const float* u_g, int cur0, int nsteps, int first, int wb_last, int R) {
+                    float* rho_g, const float* u_g, int cur0, int nsteps, int first, int wb_last, int R,
+                    int local_noslip) {
     extern __shared__ float sm[];
     cg::cluster_group cl = cg::this_cluster();
     const int c = (int)cl.block_rank();
@@ -196,7 +199,11 @@ ref_march_cluster_k(Geo g, CollideParams cp, FaceParams fp, RefNoslipPlan plan, 
                     for (int z = row0 + threadIdx.x; z < row1; z += blockDim.x) noslip_node(g, fp, v, cur, face, x, z);
                 }
             }
-            cl.sync();
+            // when every wall node's partners and their rho lie in its own
+            // CTA's rows (up/down walls, two or more rows a CTA), no other
+            // CTA takes part in this phase: a CTA barrier orders it
+            if (local_noslip) __syncthreads();
+            else cl.sync();
         }
         // ---- phase 3: east/west halo copies of this CTA's rows
         // (ref_periodic_k; D2Q9 has no north/south copy: no velocity moves
@@ -236,23 +243,60 @@ ref_march_cluster_k(Geo g, CollideParams cp, FaceParams fp, RefNoslipPlan plan, 
 
 size_t march_smem_bytes(int nx, int R) { return (size_t)(2 * Q9 + 1) * (size_t)(R + 2) * (size_t)(nx + 2) * 4; }
 
+// Threads of a CTA: one a node of its band, in whole warps, at most
+// kRefClusterThreads.
+int march_threads(int nx, int R) {
+    const long long n = ((long long)nx * R + 31) / 32 * 32;
+    return (int)(n < kRefClusterThreads ? n : kRefClusterThreads);
+}
+
+// Whether a cluster of C CTAs with this shared memory can be resident.
+bool cluster_fits(int C, int threads, size_t smem) {
+    const void* k = (const void*)ref_march_cluster_k<kArithReference>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return false;
+    if (C > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)C, 1, 1);
+    cfg.blockDim = dim3((unsigned)threads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, k, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return clusters >= 1;
+}
+
 }  // namespace
 
-// Cluster shape for a march of a D2Q9 domain (nx, nz): the fewest CTAs of
-// kRefClusterThreads threads that give every thread at most one node, within
-// the shared memory of a CTA; 0 when the domain does not fit 16 CTAs.
+// Cluster shape for a march of a D2Q9 domain (nx, nz): as many CTAs (up to
+// 16) as keep two rows or more in every CTA's band -- a step's collision is
+// issue-bound on an SM, so more SMs shorten it, and two rows keep the
+// up/down no-slip phase inside one CTA -- within a CTA's shared memory and
+// the device's cluster limits; 0 when the domain does not fit 16 CTAs.
 int ref_cluster_shape(int nx, int nz, int* C_out, int* R_out) {
     int dev = 0, smem_max = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
         return 0;
-    const long long nodes = (long long)nx * nz;
-    for (int C = 1; C <= kRefClusterMax; C *= 2) {
-        if (C < kRefClusterMax && (long long)C * kRefClusterThreads < nodes) continue;
-        if (C > nz) return 0;
+    for (int C = kRefClusterMax; C >= 1; C /= 2) {
+        if (C > 1 && nz < 2 * C) continue;
         const int R = (nz + C - 1) / C;
         if ((long long)(C - 1) * R >= nz) continue;   // every CTA owns a row
-        if (march_smem_bytes(nx, R) > (size_t)smem_max) continue;
+        if ((long long)R * nx > 4LL * kRefClusterThreads) continue;   // at most 4 nodes a thread
+        const size_t smem = march_smem_bytes(nx, R);
+        if (smem > (size_t)smem_max) continue;
+        if (!cluster_fits(C, march_threads(nx, R), smem)) continue;
         *C_out = C;
         *R_out = R;
         return 1;
@@ -264,13 +308,21 @@ int ref_march_cluster(int arith, int C, int R, const Geo& g, const CollideParams
                       const RefNoslipPlan& plan, float* b0, float* b1, float* rho, const float* u, int cur0,
                       long long nsteps, bool first, bool wb_last, cudaStream_t st) {
     const size_t smem = march_smem_bytes(g.nx, R);
+    // no-slip faces only up/down, and the first and last CTA own two rows or
+    // more: every no-slip access stays in the wall row's CTA
+    bool ud_only = true;
+    for (int i = 0; i < plan.ngroups; ++i)
+        for (int j = 0; j < plan.len[i]; ++j) ud_only &= plan.faces[i][j] >= 4;
+    const int last_rows = g.nz - (C - 1) * R;
+    const int local_noslip = (ud_only && R >= 2 && last_rows >= 2) ? 1 : 0;
+    const int threads = march_threads(g.nx, R);
     auto launch = [&](auto kernel) -> int {
         cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess && C > 8) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         if (e != cudaSuccess) return (int)e;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)C, 1, 1);
-        cfg.blockDim = dim3(kRefClusterThreads, 1, 1);
+        cfg.blockDim = dim3((unsigned)threads, 1, 1);
         cfg.dynamicSmemBytes = smem;
         cfg.stream = st;
         cudaLaunchAttribute attr[1];
@@ -290,7 +342,8 @@ int ref_march_cluster(int arith, int C, int R, const Geo& g, const CollideParams
         while (done < nsteps) {
             const long long n = nsteps - done < (1 << 20) ? nsteps - done : (1 << 20);
             e = cudaLaunchKernelEx(&cfg, kernel, g, cp, fp, plan, b0, b1, rho, u, cur, (int)n,
-                                   (int)(first && done == 0), (int)(wb_last && done + n == nsteps), R);
+                                   (int)(first && done == 0), (int)(wb_last && done + n == nsteps), R,
+                                   local_noslip);
             if (e != cudaSuccess) return (int)e;
             cur ^= (int)(n & 1);
             done += n;
