@@ -22,8 +22,9 @@ c4  512 D3Q19 domains (edges log-uniform in [16, 96], porosity 0.7-0.9),
     1,000 steps: one batch (a launch a step, graph-replayed; and all steps in
     one cooperative launch) against per-domain solves, FP32 and FP16.
 c5  the served stream: a prefix of the mixed trace and a trace of small
-    requests, each served and run as plain solves one after another, with
-    accuracy against FP64 runs (plbpd_gb300.serve_bench).
+    requests (at 200/s, and arriving at once to measure capacity), each
+    served and run as plain solves one after another, with accuracy against
+    FP64 runs (plbpd_gb300.serve_bench).
 
 Every solve is closed before the next configuration starts.
 """
@@ -229,17 +230,20 @@ def config5(mixed_requests: int = 150, small_requests: int = 300, mixed_accuracy
     out = {"workload": "Poisson arrivals at 200/s; 60 % D2Q9, 40 % D3Q19; FP32 (f - w) or FP16 (f - w) 50/50; "
                        "tau 0.55-1.5; 0-20 % solid; 500-5000 steps; 150 GB admission budget",
            "tolerance_rel_l2_u_vs_fp64": sb.TOLERANCE}
-    for label, n, small, n_acc in (("mixed_prefix", mixed_requests, False, mixed_accuracy),
-                                   ("small_requests", small_requests, True, small_requests)):
-        reqs = sb.make_requests(n, 200.0, seed, small=small)
+    for label, n, small, n_acc, rate in (("mixed_prefix", mixed_requests, False, mixed_accuracy, 200.0),
+                                         ("small_requests", small_requests, True, small_requests, 200.0),
+                                         ("small_saturated", small_requests, True, 0, 5000.0)):
+        reqs = sb.make_requests(n, rate, seed, small=small)
         masks = [sb.mask_of(r) for r in reqs]
-        idx = sorted(set(np.linspace(0, n - 1, n_acc).round().astype(int).tolist()))
+        idx = sorted(set(np.linspace(0, n - 1, n_acc).round().astype(int).tolist())) if n_acc else []
         served = sb.serve(reqs, masks, 150.0, 250, keep=idx)
         plain_run = sb.plain(reqs, masks)
         errs = sb.accuracy(reqs, masks, idx, served["results"])
         rec = sb.summarize(reqs, served, plain_run, errs)
         rec["trace"] = (f"first {n} requests of the seeded trace" if not small else
-                        f"{n} requests, D2Q9 edges 64-256 and D3Q19 edges 32-48, own seeded trace")
+                        f"{n} requests, D2Q9 edges 64-256 and D3Q19 edges 32-48, own seeded trace, "
+                        f"arrivals at {rate:g}/s" + (" (all within ~0.1 s: the server's capacity)"
+                                                    if rate > 1000 else ""))
         out[label] = rec
     return out
 

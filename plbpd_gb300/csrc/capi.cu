@@ -1308,6 +1308,12 @@ int batch_capture(plb_batch* b) {
 
 }  // namespace
 
+int plb::set_batch_multi(plb_batch* b, bool multi) {
+    if (!b) return fail(PLB_EINVAL, "batch is null");
+    b->multi = multi;
+    return PLB_OK;
+}
+
 int plb::set_batch_priority(plb_batch* b, int priority) {
     if (!b) return fail(PLB_EINVAL, "batch is null");
     PLB_CUDA(cudaSetDevice(b->device));
@@ -1385,9 +1391,10 @@ int plb_batch_create(int32_t n, plb_solve* const* solves, plb_batch** out) {
         const char* e = std::getenv("PLB_BATCH_MULTI");
         b->multi = e && std::strcmp(e, "1") == 0;
     }
+    // from pageable memory: the call returns once the tiles are staged, so
+    // the vector may go; the stream orders the copy before the first step
     if (cudaMemcpyAsync(b->d_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, b->stream) !=
-            cudaSuccess ||
-        cudaStreamSynchronize(b->stream) != cudaSuccess) {
+        cudaSuccess) {
         batch_release(b);
         return fail(PLB_ECUDA, "batch tile upload");
     }

@@ -24,6 +24,10 @@ int check_params(const plb_params* p);
 // `priority` (after the old stream's work); the solve server ranks its lanes.
 int set_solve_priority(plb_solve* s, int priority);
 int set_batch_priority(plb_batch* b, int priority);
+// Runs a batch's calls as multi-step cooperative launches (or one launch a
+// step): the solve server's lanes, whose membership changes every few
+// ticks, take one launch a tick instead of capturing a new graph.
+int set_batch_multi(plb_batch* b, bool multi);
 // rho and u of a solve in plbpd's layout (host memory), with one gather and
 // one wait for both (the solve server's retirement).
 int read_moments(plb_solve* s, float* rho, float* u);

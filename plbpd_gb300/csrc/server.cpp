@@ -50,6 +50,7 @@ int check_params(const plb_params* p);       // capi.cu: plb_solve_create's vali
 int set_solve_priority(plb_solve* s, int priority);   // capi.cu: move onto a stream of that priority
 int set_batch_priority(plb_batch* b, int priority);
 int read_moments(plb_solve* s, float* rho, float* u);   // capi.cu: rho and u with one wait
+int set_batch_multi(plb_batch* b, bool multi);          // capi.cu: one launch a call
 }
 
 namespace {
@@ -123,6 +124,14 @@ int64_t active_cells_cap() {
         const char* e = std::getenv("PLB_SERVER_ACTIVE_CELLS");
         const long long x = e ? std::atoll(e) : 0;
         return (int64_t)(x > 0 ? x : (1LL << 23));
+    }();
+    return v;
+}
+
+bool server_batch_multi() {
+    static const bool v = [] {
+        const char* e = std::getenv("PLB_SERVER_BATCH_MULTI");
+        return !(e && std::strcmp(e, "0") == 0);
     }();
     return v;
 }
@@ -284,6 +293,12 @@ void launch_tick(plb_server* srv, Lane& L) {
             if (plb_batch_create((int32_t)ss.size(), ss.data(), &L.batch) != PLB_OK)
                 return fail_lane(srv, L, plb_last_error());
             if (plb::set_batch_priority(L.batch, srv->prio_greatest) != PLB_OK)
+                return fail_lane(srv, L, plb_last_error());
+            // a lane's membership changes every few ticks: one cooperative
+            // launch a tick costs the scheduler microseconds where capturing
+            // a new graph for each membership costs milliseconds
+            // (PLB_SERVER_BATCH_MULTI=0: graph chunks)
+            if (plb::set_batch_multi(L.batch, server_batch_multi()) != PLB_OK)
                 return fail_lane(srv, L, plb_last_error());
             L.dirty = false;
             srv->t_rebuild += std::chrono::duration<double>(Clock::now() - tr).count();
