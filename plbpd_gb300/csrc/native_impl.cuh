@@ -764,12 +764,15 @@ __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, c
     uint8_t t0 = 0, t1 = 0;
     uint32_t L0 = 0, L1 = 0;
     if (MASK && active) {
+        // the pair's two link words are read beside its types, not after
+        // them: the fix-up loads wait for one round trip instead of two
         const unsigned short tt = __ldg(reinterpret_cast<const unsigned short*>(types + node0));
+        const uint2 lw = __ldg(reinterpret_cast<const uint2*>(np.links + node0));
         t0 = (uint8_t)(tt & 0xff);
         t1 = (uint8_t)(tt >> 8);
         skip = (t0 & kSolid) && (t1 & kSolid);
-        L0 = links_of<MASK>(t0, np.links, node0);
-        L1 = links_of<MASK>(t1, np.links, node0 + 1);
+        L0 = (t0 & kNearSolid) ? lw.x : 0u;
+        L1 = (t1 & kNearSolid) ? lw.y : 0u;
     }
     float2 f[Q];   // .x node x0, .y node x0 + 1
 #pragma unroll
