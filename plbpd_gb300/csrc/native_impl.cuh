@@ -701,12 +701,14 @@ nat_fused_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::
     const long long node = g.idx(x, y, z);
     // the type is read first: loading a solid node's sources would cost
     // traffic in obstacle-filled regions (measured 15% slower on D3Q27 with
-    // 15% solid spheres), more than the round trip it saves
+    // 15% solid spheres), more than the round trip it saves; the link word
+    // is read beside it, so the bounce-back fix-ups wait one round trip less
     uint32_t L = 0;
     if (MASK) {
         const uint8_t t = __ldg(types + node);
+        const uint32_t lw = __ldg(np.links + node);
         if (t & kSolid) return;
-        L = links_of<MASK>(t, np.links, node);
+        L = (t & kNearSolid) ? lw : 0u;
     }
     const Nbr nb(g, x, y, z);
     R f[Q];
@@ -1135,10 +1137,11 @@ __device__ __forceinline__ void batch_tasks(const BatchDomain* __restrict__ doms
         const int y = (int)((unsigned)i / (unsigned)g.nx), x = i - y * g.nx, z = tk.y;
         const long long node = g.idx(x, y, z);
         const uint8_t* types = D.types;
-        const uint8_t tt = __ldg(types + node);
-        if (tt & kSolid) continue;
         const NativeParams& np = D.np;
-        const uint32_t L = links_of<true>(tt, np.links, node);
+        const uint8_t tt = __ldg(types + node);
+        const uint32_t lw = __ldg(np.links + node);   // beside the type, as nat_fused_k
+        if (tt & kSolid) continue;
+        const uint32_t L = (tt & kNearSolid) ? lw : 0u;
         const T* src = static_cast<const T*>(D.f[parity]);
         T* dst = static_cast<T*>(D.f[parity ^ 1]);
         const Nbr nb(g, x, y, z);
