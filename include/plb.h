@@ -207,12 +207,16 @@ void* plb_stream_handle(plb_solve* s);
  * The NATIVE fused step with even nx comes in several compiled variants that
  * give bit-identical results: for FP16 storage seven forms of the two-node
  * pair kernel, for FP32 (FP32 arithmetic) and FP32_DEV storage the one-node
- * kernel and three forms of the pair kernel.  Before a solve's first fused
- * step the library times each on the solve's own buffers
- * (the trial steps write only the buffer the next step overwrites) and keeps
- * the fastest per lattice, storage, collision, mask, block width and size
- * class (floor(log2 cells)) for the process; PLB_TUNE_CACHE=<file> keeps the
- * table across processes, PLB_TUNE=0 uses variant 0.  No plbpd counterpart:
+ * kernel and three forms of the pair kernel, for FP32 storage with plbpd's
+ * arithmetic the one-node kernel and one form of the pair kernel.  Before a
+ * solve's first fused step the library times each on the solve's own
+ * buffers (the trial steps write only the buffer the next step overwrites)
+ * and keeps the fastest per lattice, storage, collision, mask, block width
+ * and size class (floor(log2 cells)) for the process; PLB_TUNE_CACHE=<file>
+ * keeps the table across processes, PLB_TUNE=0 uses variant 0.  A choice
+ * made by trials is timed once more after 256 fused steps, on the state the
+ * solve has reached (a flow started from rest can favour another variant for
+ * its first steps than for the rest of the run).  No plbpd counterpart:
  * plbpd's TBB loops have no launch configuration to tune. */
 /* Number of variants the library compiles (valid ids are 0 .. n-1). */
 int plb_tune_variants(void);
@@ -222,6 +226,14 @@ int plb_tune_variants(void);
 int plb_tune_force(int32_t variant);
 /* The variant the solve runs, or -1 before its first fused step. */
 int plb_tune_variant(const plb_solve* s, int32_t* variant);
+/* Times the variants on the solve's current state now (synchronises the
+ * solve's stream), keeps the fastest for this solve and records it in the
+ * table; no later trial follows.  A caller that times its own steps calls
+ * it after its warm-up so that no trial falls in the timed steps.  No-op
+ * (PLB_OK) for REFERENCE semantics and AA streaming; under plb_tune_force or
+ * PLB_TUNE=0 it takes that variant.  Must not be called while the stream is
+ * being captured. */
+int plb_tune(plb_solve* s);
 
 /* ---- batches of solves --------------------------------------------------------
  * A batch advances many NATIVE solves of one lattice, storage and device

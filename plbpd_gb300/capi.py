@@ -63,6 +63,7 @@ _SIGS = [
     ("plb_tune_variants", C.c_int, []),
     ("plb_tune_force", C.c_int, [C.c_int32]),
     ("plb_tune_variant", C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+    ("plb_tune", C.c_int, [C.c_void_p]),
     ("plb_collide", C.c_int, [C.c_void_p]),
     ("plb_stream_push", C.c_int, [C.c_void_p]),
     ("plb_apply_noslip", C.c_int, [C.c_void_p]),
@@ -237,6 +238,12 @@ class Solve:
         v = C.c_int32()
         check(lib().plb_tune_variant(self.h, C.byref(v)))
         return v.value
+
+    def tune(self) -> int:
+        """Times the fused-step variants on the current state now, keeps the
+        fastest (no later trial) and returns it."""
+        check(lib().plb_tune(self.h))
+        return self.variant()
     def collide(self) -> None: check(lib().plb_collide(self.h))
     def stream_push(self) -> None: check(lib().plb_stream_push(self.h))
     def apply_noslip(self) -> None: check(lib().plb_apply_noslip(self.h))

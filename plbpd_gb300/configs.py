@@ -127,6 +127,7 @@ def config2(peak_gbs: float, steps: int = 2000, n_side: int = 256, forms=None) -
             continue
         with _periodic_solve(n_side, storage, arith, start) as s:
             s.step(warm)
+            s.tune()
             sec = _timed(s, steps - warm)
             rho, u = _fields(s)
             mlups = _mlups(cells, steps - warm, sec)
@@ -157,6 +158,7 @@ def config3(peak_gbs: float, steps: int = 5000, fp32_steps: int = 500, accuracy_
                                          ("fp32_storage", capi.STORAGE_FP32, fp32_steps, 217)):
         with _duct_solve(n, storage, mask) as s:
             s.step(3)
+            s.tune()
             sec = _timed(s, st_steps)
             mlups = _mlups(cells, st_steps, sec)
             out[name] = {"steps": st_steps, "mlups": mlups, "bytes_per_cell": bpc,
@@ -206,6 +208,13 @@ def config4(steps: int = 1000, domains: int = 512, storages=("fp32", "fp16"), se
                 del os.environ["PLB_BATCH_MULTI"]
             else:
                 os.environ["PLB_BATCH_MULTI"] = prev
+        # each size class's kernel variant timed before the per-domain steps
+        classes = set()
+        for s in solves:
+            c = (s.nx * s.ny * s.nz).bit_length()
+            if c not in classes:
+                classes.add(c)
+                s.tune()
         for s in solves:
             s.synchronize()
         t0 = time.perf_counter()

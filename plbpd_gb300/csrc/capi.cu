@@ -148,6 +148,10 @@ struct plb_solve {
     int64_t device_bytes = 0;
     // variant of the fused-step kernel (autotuner); -1 until chosen
     int variant = -1;
+    // fused steps marched since the solve was made, and the count at which
+    // the variants are timed once more (-1: no second trial)
+    int64_t fused_steps = 0;
+    int64_t retune_at = -1;
 };
 
 namespace {
@@ -421,9 +425,9 @@ int ref_materialize_fields(plb_solve* s) {
 // ---- autotuner of the fused-step kernel --------------------------------------
 // The NATIVE fused step with even nx is compiled in several variants that
 // give the same bits (native_impl.cuh: kH2Variant for FP16 storage; the
-// one-node kernel and the pair kernel's forms for FP32 and FP32_DEV); which
-// is fastest depends on the lattice, the mask, the block width and the
-// domain size.  Before a solve's
+// one-node kernel and the pair kernel's forms for FP32 and FP32_DEV, either
+// arithmetic); which is fastest depends on the lattice, the mask, the block
+// width and the domain size.  Before a solve's
 // first fused step the variants are timed on the solve's own buffers: a pull
 // step reads buffer cur and writes the other one, which the next real step
 // overwrites, so trial launches leave the state as it was.  The winner is
@@ -431,6 +435,17 @@ int ref_materialize_fields(plb_solve* s) {
 // size class = floor(log2 cells)) for the process, and in the file named by
 // PLB_TUNE_CACHE across processes.  PLB_TUNE=0 turns tuning off (variant 0);
 // plb_tune_force fixes one variant.
+//
+// The state a solve starts from can favour another variant than the state
+// it runs in: with plbpd's arithmetic a masked flow at rest sends many tail
+// evaluations to the FP64 fallback for its first steps, where the one-node
+// kernel is faster, and the pair kernel is faster from then on.  So a
+// choice made by trials is timed once more after kRetuneSteps fused steps,
+// on the state the solve has reached, and that choice is kept (graphs
+// captured with the first are dropped).  plb_tune times the variants on
+// the current state at a moment the caller picks, and no second trial
+// follows it.
+constexpr int64_t kRetuneSteps = 256;
 using TuneKey = std::array<int, 7>;
 std::mutex g_tune_mu;
 std::map<TuneKey, int> g_tune;
@@ -502,45 +517,87 @@ int time_variant(plb_solve* s, int v, int reps, cudaEvent_t e0, cudaEvent_t e1, 
     return PLB_OK;
 }
 
-// Sets s->variant (not during a graph capture: the trials synchronise).
-int choose_variant(plb_solve* s) {
-    const int nv = fused_variants(s);
-    const int forced = g_tune_force.load();
-    if (nv <= 1) { s->variant = 0; return PLB_OK; }
-    if (forced >= 0) { s->variant = forced < nv ? forced : 0; return PLB_OK; }
-    const char* on = std::getenv("PLB_TUNE");
-    if (on && std::strcmp(on, "0") == 0) { s->variant = 0; return PLB_OK; }
+TuneKey tune_key(const plb_solve* s) {
     const long long cells = (long long)s->g.nx * s->g.ny * s->g.nz;
     int cls = 0;
     while ((2LL << cls) <= cells) ++cls;
-    const TuneKey key = {s->q, s->storage, s->karith, (int)s->has_mask, (int)(s->has_mask && s->np.moving),
-                         (int)(s->g.nx % 256 == 0), cls};
-    {
-        std::lock_guard<std::mutex> lk(g_tune_mu);
-        tune_load_locked();
-        auto it = g_tune.find(key);
-        if (it != g_tune.end() && it->second < nv) { s->variant = it->second; return PLB_OK; }
-    }
-    // about 2^25 node updates a trial, 3 to 50 launches
+    return {s->q, s->storage, s->karith, (int)s->has_mask, (int)(s->has_mask && s->np.moving),
+            (int)(s->g.nx % 256 == 0), cls};
+}
+
+// The variant a solve takes without trials: 0 for one variant or PLB_TUNE=0,
+// the forced one, or -1 (trials decide).
+int untimed_variant(const plb_solve* s, int nv) {
+    const int forced = g_tune_force.load();
+    if (nv <= 1) return 0;
+    if (forced >= 0) return forced < nv ? forced : 0;
+    const char* on = std::getenv("PLB_TUNE");
+    if (on && std::strcmp(on, "0") == 0) return 0;
+    return -1;
+}
+
+// Times every variant on the solve's current state, sets s->variant to the
+// fastest and records it (not during a graph capture: the trials
+// synchronise).
+int tune_trials(plb_solve* s, int nv) {
+    const long long cells = (long long)s->g.nx * s->g.ny * s->g.nz;
+    // about 2^25 node updates a trial, 3 to 50 launches; two passes over the
+    // variants, the second in reverse order, and each variant's faster pass
+    // counts, so a clock that is still rising or another process's burst
+    // does not decide the choice
     const long long r = (1LL << 25) / (cells > 0 ? cells : 1);
     const int reps = r < 3 ? 3 : (r > 50 ? 50 : (int)r);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     PLB_CUDA(cudaEventCreate(&e0));
     if (cudaEventCreate(&e1) != cudaSuccess) { cudaEventDestroy(e0); return fail(PLB_ECUDA, "cudaEventCreate"); }
-    int best = 0, rc = PLB_OK;
-    float best_ms = 0.0f;
-    for (int v = 0; v < nv && rc == PLB_OK; ++v) {
-        float ms = 0.0f;
-        rc = time_variant(s, v, reps, e0, e1, &ms);
-        if (rc == PLB_OK && (v == 0 || ms < best_ms)) { best = v; best_ms = ms; }
+    std::vector<float> best_of(nv, 0.0f);
+    int rc = PLB_OK;
+    for (int pass = 0; pass < 2 && rc == PLB_OK; ++pass) {
+        for (int i = 0; i < nv && rc == PLB_OK; ++i) {
+            const int v = pass == 0 ? i : nv - 1 - i;
+            float ms = 0.0f;
+            rc = time_variant(s, v, reps, e0, e1, &ms);
+            if (rc == PLB_OK && (pass == 0 || ms < best_of[v])) best_of[v] = ms;
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc != PLB_OK) return rc;
+    int best = 0;
+    for (int v = 1; v < nv; ++v)
+        if (best_of[v] < best_of[best]) best = v;
+    if (best != s->variant) drop_graphs(s);   // captured with the other variant
     s->variant = best;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    tune_store_locked(key, best);
+    tune_store_locked(tune_key(s), best);
     return PLB_OK;
+}
+
+// Sets s->variant before the solve's first fused step: untimed, from the
+// table, or by trials (then timed again after kRetuneSteps fused steps).
+int choose_variant(plb_solve* s) {
+    const int nv = fused_variants(s);
+    const int fixed = untimed_variant(s, nv);
+    if (fixed >= 0) { s->variant = fixed; return PLB_OK; }
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        tune_load_locked();
+        auto it = g_tune.find(tune_key(s));
+        if (it != g_tune.end() && it->second < nv) { s->variant = it->second; return PLB_OK; }
+    }
+    PLB_TRY(tune_trials(s, nv));
+    s->retune_at = s->fused_steps + kRetuneSteps;
+    return PLB_OK;
+}
+
+// The second trial of a choice made by trials, once the solve has marched
+// kRetuneSteps fused steps.
+int maybe_retune(plb_solve* s) {
+    if (s->retune_at < 0 || s->fused_steps < s->retune_at) return PLB_OK;
+    s->retune_at = -1;
+    const int nv = fused_variants(s);
+    if (untimed_variant(s, nv) >= 0) return PLB_OK;
+    return tune_trials(s, nv);
 }
 
 // ---- NATIVE semantics ------------------------------------------------------
@@ -683,8 +740,18 @@ int march(plb_solve* s, int64_t n) {
         s->post = true;
         done = 1;
     }
-    while (G > 0 && n - done >= G) { PLB_TRY(run_chunk(s)); done += G; }
-    while (done < n) { PLB_TRY(nat_one_step(s)); ++done; }
+    while (done < n) {
+        PLB_TRY(maybe_retune(s));
+        if (G > 0 && n - done >= G) {
+            PLB_TRY(run_chunk(s));
+            done += G;
+            s->fused_steps += G;
+        } else {
+            PLB_TRY(nat_one_step(s));
+            ++done;
+            ++s->fused_steps;
+        }
+    }
     return PLB_OK;
 }
 
@@ -950,6 +1017,21 @@ int plb_tune_variant(const plb_solve* s, int32_t* variant) {
     if (!s || !variant) return fail(PLB_EINVAL, "null argument");
     *variant = s->variant;
     return PLB_OK;
+}
+
+int plb_tune(plb_solve* s) {
+    if (!s) return fail(PLB_EINVAL, "solve is null");
+    PLB_TRY(set_device(s));
+    s->retune_at = -1;
+    if (!s->native || s->aa) return PLB_OK;   // one kernel form, nothing to time
+    const int nv = fused_variants(s);
+    const int fixed = untimed_variant(s, nv);
+    if (fixed >= 0) {
+        if (fixed != s->variant) drop_graphs(s);
+        s->variant = fixed;
+        return PLB_OK;
+    }
+    return tune_trials(s, nv);
 }
 
 int plb_step(plb_solve* s, int64_t nsteps) {

@@ -126,14 +126,18 @@ int nat_fused_h2_bgk19(bool mask, const Geo& g, const CollideParams& cp, const N
                        void* dst, const uint8_t* types, int variant, cudaStream_t st);
 int nat_fused_h2_bgk27(bool mask, const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src,
                        void* dst, const uint8_t* types, int variant, cudaStream_t st);
-// The FP32 / FP32-deviation pair kernel (storage 0 with FP32 arithmetic, or
-// 3) of one lattice, variants 1-3 of nat_fused_step (kernels_pair32_q<Q>.cu).
-int nat_fused_pair32_q9(int storage, bool mask, const Geo& g, const CollideParams& cp, const NativeParams& np,
-                        const void* src, void* dst, const uint8_t* types, int variant, cudaStream_t st);
-int nat_fused_pair32_q19(int storage, bool mask, const Geo& g, const CollideParams& cp, const NativeParams& np,
-                         const void* src, void* dst, const uint8_t* types, int variant, cudaStream_t st);
-int nat_fused_pair32_q27(int storage, bool mask, const Geo& g, const CollideParams& cp, const NativeParams& np,
-                         const void* src, void* dst, const uint8_t* types, int variant, cudaStream_t st);
+// The FP32 / FP32-deviation pair kernel (storage 0 with FP32 or plbpd's
+// arithmetic, or 3) of one lattice: variants 1-3 of nat_fused_step with FP32
+// arithmetic, variant 1 with plbpd's (kernels_pair32_q<Q>.cu).
+int nat_fused_pair32_q9(int storage, int arith, bool mask, const Geo& g, const CollideParams& cp,
+                        const NativeParams& np, const void* src, void* dst, const uint8_t* types, int variant,
+                        cudaStream_t st);
+int nat_fused_pair32_q19(int storage, int arith, bool mask, const Geo& g, const CollideParams& cp,
+                         const NativeParams& np, const void* src, void* dst, const uint8_t* types, int variant,
+                         cudaStream_t st);
+int nat_fused_pair32_q27(int storage, int arith, bool mask, const Geo& g, const CollideParams& cp,
+                         const NativeParams& np, const void* src, void* dst, const uint8_t* types, int variant,
+                         cudaStream_t st);
 // Gather only: writes n (storage format, or nullptr) and the moments with the
 // solid-node resets (rho/u, or nullptr).
 int nat_gather(int q, int storage, bool has_mask, const Geo& g, const NativeParams& np,

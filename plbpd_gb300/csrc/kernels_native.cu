@@ -100,6 +100,7 @@ int nat_fused_variants(int q, int storage, int arith, bool moving, const Geo& g)
     if (g.nx % 2 != 0) return 1;
     if (storage == 1) return nat_h2_variant_count(q, arith, moving);
     if ((storage == 3 && arith != kArithTRT) || (storage == 0 && arith == kArithFP32)) return moving ? 1 : kPair32Variants;
+    if (storage == 0 && arith == kArithReference) return moving ? 1 : kPairRefVariants;
     return 1;
 }
 

@@ -1319,23 +1319,32 @@ int launch_fused_h2(const Geo& g, const CollideParams& cp, const NativeParams& n
 
 // FP32 and FP32-deviation storage (BGK, FP32 arithmetic) with even nx: the
 // single-node kernel is variant 0, the pair kernel in forms 0, 1 and 2 are
-// variants 1-3.  Moving walls and other arithmetics have the single-node
-// kernel only.
+// variants 1-3.  FP32 storage with plbpd's arithmetic has the single-node
+// kernel and the pair kernel in form 2 (each node's own update, so the
+// exact-tail emulation and its FP64 fallback run per node as in the
+// single-node kernel): variants 0 and 1.  Moving walls, FP64 storage and TRT
+// have the single-node kernel only.
 constexpr int kPair32Variants = 4;
+constexpr int kPairRefVariants = 2;
 
-template <int Q, int ST, bool MASK>
+template <int Q, int ST, bool MASK, int ARITH = kArithFP32>
 int launch_fused_pair32(const Geo& g, const CollideParams& cp, const NativeParams& np, const void* src, void* dst,
                         const uint8_t* types, int variant, cudaStream_t st) {
     static_assert(ST == 0 || ST == 3, "FP32 storages only");
+    static_assert(ARITH == kArithFP32 || (ARITH == kArithReference && ST == 0), "BGK arithmetics of FP32 storage");
     using T = typename Store<ST>::T;
     auto s2 = (const T*)src;
     auto d2 = (T*)dst;
     auto go = [&](auto bxc) {
         constexpr int BX = decltype(bxc)::value;
         const dim3 grid = seg_grid(g, BX, 2);
-        if (variant == 2) nat_fused_h2_k<Q, MASK, false, kArithFP32, BX, 1, ST><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types);
-        else if (variant == 3) nat_fused_h2_k<Q, MASK, false, kArithFP32, BX, 2, ST><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types);
-        else nat_fused_h2_k<Q, MASK, false, kArithFP32, BX, 0, ST><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types);
+        if constexpr (ARITH == kArithReference) {
+            nat_fused_h2_k<Q, MASK, false, ARITH, BX, 2, ST><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types);
+        } else {
+            if (variant == 2) nat_fused_h2_k<Q, MASK, false, ARITH, BX, 1, ST><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types);
+            else if (variant == 3) nat_fused_h2_k<Q, MASK, false, ARITH, BX, 2, ST><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types);
+            else nat_fused_h2_k<Q, MASK, false, ARITH, BX, 0, ST><<<grid, BX, 0, st>>>(g, cp, np, s2, d2, types);
+        }
     };
     if (block_x(g, 2) == kBlockX) go(std::integral_constant<int, kBlockX>{});
     else go(std::integral_constant<int, 32>{});
@@ -1360,11 +1369,11 @@ int fused_q(int storage, int arith, bool m, const Geo& g, const CollideParams& c
                 }
             }
         }
-        if constexpr (!TRT && (ST == 3 || (ST == 0 && AR == kArithFP32))) {
+        if constexpr (!TRT && (ST == 3 || ST == 0)) {
             if (variant > 0 && g.nx % 2 == 0 && !(m && np.moving)) {
-                if constexpr (Q == 9) return nat_fused_pair32_q9(ST, m, g, cp, np, src, dst, types, variant, st);
-                if constexpr (Q == 19) return nat_fused_pair32_q19(ST, m, g, cp, np, src, dst, types, variant, st);
-                if constexpr (Q == 27) return nat_fused_pair32_q27(ST, m, g, cp, np, src, dst, types, variant, st);
+                if constexpr (Q == 9) return nat_fused_pair32_q9(ST, AR, m, g, cp, np, src, dst, types, variant, st);
+                if constexpr (Q == 19) return nat_fused_pair32_q19(ST, AR, m, g, cp, np, src, dst, types, variant, st);
+                if constexpr (Q == 27) return nat_fused_pair32_q27(ST, AR, m, g, cp, np, src, dst, types, variant, st);
             }
         }
         return m ? launch_fused<Q, ST, true, AR>(g, cp, np, src, dst, types, st)

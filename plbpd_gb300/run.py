@@ -90,6 +90,7 @@ def main(argv=None):
             s.set_mask(sphere_mask(int(p.nx), int(p.ny), int(p.nz)))
         s.initialize()
         s.step(a.warmup)
+        s.tune()
         s.synchronize()
         t0 = time.perf_counter()
         s.step(a.steps)

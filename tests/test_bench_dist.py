@@ -42,3 +42,18 @@ def test_aggregate_two_gloo_ranks():
             assert p.exitcode == 0
         for r in range(world):
             assert out[r] == (15.0, 3000.0)   # max over ranks, sum over ranks
+
+
+def test_traffic_figures_match_their_profiles():
+    """Each DRAM-traffic figure bench.py reports comes from the committed ncu
+    summary it names, which states the same number."""
+    import re
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    import bench
+    for key, (traffic, path) in bench.TRAFFIC.items():
+        assert key in bench.KERNELS, key
+        with open(os.path.join(root, path)) as f:
+            figures = [int(v) for v in re.findall(r"traffic_bytes_per_launch\[[^\]]*\]: (\d+)", f.read())]
+        assert traffic in figures, (key, path)
