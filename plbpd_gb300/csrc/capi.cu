@@ -898,8 +898,8 @@ int plb_solve_create(const plb_params* params, plb_solve** out) {
         s->np.links = s->links;
         if (cudaMemsetAsync(s->types, 0, (size_t)g.ks, s->stream) != cudaSuccess)
             return bail(fail(PLB_ECUDA, "cudaMemsetAsync(types)"));
-        const int e = nat_build_types(s->q, g, nullptr, s->fp.noslip_mask, s->types_tmp, s->types, s->links,
-                                      s->stream);
+        const int e = nat_build_types(s->q, g, nullptr, s->fp.noslip_mask, (int)esize_of(s->storage), s->types_tmp,
+                                      s->types, s->links, s->stream);
         if (e != 0) return bail(fail(PLB_ECUDA, "nat_build_types"));
         s->post = false;
     }
@@ -974,9 +974,8 @@ int plb_set_mask(plb_solve* s, const uint8_t* mask) {
     const size_t cells = (size_t)s->g.cells();
     if (!s->mask_dev) PLB_TRY(dalloc(s, (void**)&s->mask_dev, cells));
     if (mask) PLB_CUDA(cudaMemcpyAsync(s->mask_dev, mask, cells, cudaMemcpyHostToDevice, s->stream));
-    PLB_KERNEL(nat_build_types(s->q, s->g, mask ? s->mask_dev : nullptr, s->fp.noslip_mask, s->types_tmp, s->types,
-                               s->links,
-                               s->stream));
+    PLB_KERNEL(nat_build_types(s->q, s->g, mask ? s->mask_dev : nullptr, s->fp.noslip_mask,
+                               (int)esize_of(s->storage), s->types_tmp, s->types, s->links, s->stream));
     s->has_mask = mask != nullptr || s->fp.noslip_mask != 0;
     drop_graphs(s);
     return sync(s);

@@ -48,6 +48,12 @@ struct FaceParams {
 //          6 = obstacle, zero velocity)
 //   bit 6: fluid node with at least one solid neighbour
 enum : uint8_t { kSolid = 0x80, kNearSolid = 0x40, kVelMask = 0x07, kObstacleVel = 6 };
+// A solid node whose 32-byte sector of its row (in the population storage)
+// also holds a fluid node: the fused kernels store into its slots (values
+// that no fluid node reads) so that the sector is written whole.  A partly
+// written sector makes the memory system read the sector from DRAM before
+// it writes it back.
+enum : uint8_t { kSectorMate = 0x20 };
 
 struct NativeParams {
     float vel[8][3];      // solid velocities by index (6 = obstacle = 0)
@@ -157,8 +163,9 @@ int nat_aa_gather(int q, int storage, bool has_mask, bool swapped, const Geo& g,
 int nat_reset_fields(const Geo& g, const NativeParams& np, const uint8_t* types, float* rho,
                      float* u, cudaStream_t st);
 // Node types from an obstacle mask (nz*ny*nx bytes, may be null) and the walls.
-// `scratch` has the size of `types`; `links` gets one word per node.
-int nat_build_types(int q, const Geo& g, const uint8_t* mask, int noslip_mask,
+// `scratch` has the size of `types`; `links` gets one word per node; esize:
+// bytes of one stored population (for kSectorMate).
+int nat_build_types(int q, const Geo& g, const uint8_t* mask, int noslip_mask, int esize,
                     uint8_t* scratch, uint8_t* types, uint32_t* links, cudaStream_t st);
 
 // ---- batches of NATIVE domains (kernels_native.cu) --------------------------

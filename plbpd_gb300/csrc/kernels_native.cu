@@ -45,7 +45,7 @@ nat_types_solid_k(Geo g, const uint8_t* __restrict__ mask, int noslip_mask, uint
 template <int Q>
 __global__ void __launch_bounds__(kBlockX)
 nat_types_near_k(Geo g, const uint8_t* __restrict__ types, uint8_t* __restrict__ out,
-                 uint32_t* __restrict__ links) {
+                 uint32_t* __restrict__ links, int esize) {
     const int x = blockIdx.x * kBlockX + threadIdx.x;
     const int y = blockIdx.y, z = blockIdx.z;
     if (x >= g.nx) return;
@@ -53,7 +53,17 @@ nat_types_near_k(Geo g, const uint8_t* __restrict__ types, uint8_t* __restrict__
     const uint8_t t = types[node];
     out[node] = t;
     links[node] = 0u;
-    if (t & kSolid) return;
+    if (t & kSolid) {
+        // rows start on a 32-byte boundary (the row pitch is a whole number of
+        // sectors), so the sector of x is the run of 32 / esize nodes holding it
+        const int S = 32 / esize, x0 = x - x % S, x1 = min(x0 + S, g.nx);
+        for (int xx = x0; xx < x1; ++xx)
+            if (!(types[node - x + xx] & kSolid)) {
+                out[node] = t | kSectorMate;
+                break;
+            }
+        return;
+    }
     const Nbr nb(g, x, y, z);
     uint32_t bits = 0u;   // bit k: x + c_k is solid
 #pragma unroll
@@ -207,10 +217,10 @@ int nat_reset_fields(const Geo& g, const NativeParams& np, const uint8_t* types,
     return (int)cudaGetLastError();
 }
 
-int nat_build_types(int q, const Geo& g, const uint8_t* mask, int noslip_mask, uint8_t* scratch,
+int nat_build_types(int q, const Geo& g, const uint8_t* mask, int noslip_mask, int esize, uint8_t* scratch,
                     uint8_t* types, uint32_t* links, cudaStream_t st) {
 #define CALL(Q) (nat_types_solid_k<Q><<<cell_grid(g), kBlockX, 0, st>>>(g, mask, noslip_mask, scratch), \
-                 nat_types_near_k<Q><<<cell_grid(g), kBlockX, 0, st>>>(g, scratch, types, links), \
+                 nat_types_near_k<Q><<<cell_grid(g), kBlockX, 0, st>>>(g, scratch, types, links, esize), \
                  (int)cudaGetLastError())
     return PLB_Q_DISPATCH(q, CALL);
 #undef CALL

@@ -76,6 +76,8 @@ def main(argv=None):
     ap.add_argument("--spheres", action="store_true")
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--no-tune", action="store_true",
+                    help="no timed trials after the warm-up: keep the variant of the first fused step (for profiling)")
     ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16", "fp32dev", "fp64"])
     ap.add_argument("--collision", default="bgk", choices=["bgk", "trt"])
     ap.add_argument("--arith", default="fp32", choices=["fp32", "reference"])
@@ -90,7 +92,8 @@ def main(argv=None):
             s.set_mask(sphere_mask(int(p.nx), int(p.ny), int(p.nz)))
         s.initialize()
         s.step(a.warmup)
-        s.tune()
+        if not a.no_tune:
+            s.tune()   # the kernel variant timed on the warmed-up state, before the timed steps
         s.synchronize()
         t0 = time.perf_counter()
         s.step(a.steps)
