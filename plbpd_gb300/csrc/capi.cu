@@ -1276,7 +1276,9 @@ struct plb_batch {
     BatchDomain* d_doms = nullptr;
     int4* d_tiles = nullptr;   // warp tasks (domain, z, first node of the plane, 1 for a pair task)
     int ntiles = 0;
-    int blocks = 0;
+    int npair = 0;             // the first npair tasks are pair tasks
+    int blocks = 0;            // the multi-step kernel's grid (both kinds in one kernel)
+    int blocks_pair = 0, blocks_single = 0;   // the one-step kernels' grids
     int64_t cells = 0;
     bool moving = false;   // some member has a moving wall
     bool pairs = false;    // some domain has even nx: 64-node pair tasks beside 32-node ones
@@ -1373,8 +1375,8 @@ int batch_capture(plb_batch* b) {
     PLB_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     int rc = 0;
     for (int i = 0; i < b->graph_steps && rc == 0; ++i)
-        rc = nat_batch_step(b->q, b->storage, b->arith, b->moving, b->pairs, b->d_doms, b->d_tiles, b->ntiles, i & 1,
-                            b->blocks, b->stream);
+        rc = nat_batch_step(b->q, b->storage, b->arith, b->moving, b->d_doms, b->d_tiles, b->ntiles, b->npair, i & 1,
+                            b->blocks_pair, b->blocks_single, b->stream);
     const cudaError_t ec = cudaStreamEndCapture(b->stream, &graph);
     if (rc != 0) {
         if (graph) cudaGraphDestroy(graph);
@@ -1437,24 +1439,35 @@ int plb_batch_create(int32_t n, plb_solve* const* solves, plb_batch** out) {
         batch_release(b);
         return fail(PLB_ECUDA, "cudaEventCreate");
     }
-    // a domain with even nx runs as pair tasks (two nodes a lane, 64 a warp)
+    // a domain with even nx runs as pair tasks (two nodes a lane, 64 a warp),
+    // listed first: each kind has its own kernel
     std::vector<int4> tiles;
-    for (int i = 0; i < n; ++i) {
-        const Geo& g = solves[i]->g;
-        const bool pair = g.nx % 2 == 0;
-        const int per_task = pair ? 64 : 32;
-        b->pairs |= pair;
-        const int plane = g.nx * g.ny;   // nodes of one z plane, x fastest
-        for (int z = 0; z < g.nz; ++z)
-            for (int i0 = 0; i0 < plane; i0 += per_task) tiles.push_back(make_int4(i, z, i0, pair ? 1 : 0));
-        b->cells += g.cells();
+    for (int kind = 1; kind >= 0; --kind) {
+        for (int i = 0; i < n; ++i) {
+            const Geo& g = solves[i]->g;
+            const bool pair = g.nx % 2 == 0;
+            if ((int)pair != kind) continue;
+            const int per_task = pair ? 64 : 32;
+            b->pairs |= pair;
+            const int plane = g.nx * g.ny;   // nodes of one z plane, x fastest
+            for (int z = 0; z < g.nz; ++z)
+                for (int i0 = 0; i0 < plane; i0 += per_task) tiles.push_back(make_int4(i, z, i0, pair ? 1 : 0));
+            b->cells += g.cells();
+        }
+        if (kind == 1) b->npair = (int)tiles.size();
     }
     b->ntiles = (int)tiles.size();
     int dev_sms = 0;
     cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, b->device);
+    if (dev_sms < 1) dev_sms = 1;
     for (int i = 0; i < n; ++i) b->moving |= solves[i]->np.moving != 0;
-    const int per_sm = nat_batch_blocks_per_sm(b->q, b->storage, b->arith, b->moving, b->pairs);
-    b->blocks = (dev_sms > 0 ? dev_sms : 1) * (per_sm > 0 ? per_sm : 1);
+    auto grid_of = [&](int kind) {
+        const int per_sm = nat_batch_blocks_per_sm(b->q, b->storage, b->arith, b->moving, kind);
+        return dev_sms * (per_sm > 0 ? per_sm : 1);
+    };
+    b->blocks = grid_of(b->pairs ? 2 : 0);
+    b->blocks_pair = grid_of(1);
+    b->blocks_single = grid_of(0);
     // stream-ordered, like a solve's memory
     if (cudaMallocAsync(&b->d_doms, n * sizeof(BatchDomain), b->stream) != cudaSuccess ||
         cudaMallocAsync(&b->d_tiles, tiles.size() * sizeof(int4), b->stream) != cudaSuccess ||
@@ -1525,8 +1538,8 @@ int plb_batch_step_async(plb_batch* b, int64_t nsteps) {
         i += G;
     }
     for (; i < todo; ++i)
-        PLB_KERNEL(nat_batch_step(b->q, b->storage, b->arith, b->moving, b->pairs, b->d_doms, b->d_tiles, b->ntiles, (int)(i & 1),
-                                  b->blocks, b->stream));
+        PLB_KERNEL(nat_batch_step(b->q, b->storage, b->arith, b->moving, b->d_doms, b->d_tiles, b->ntiles, b->npair,
+                                  (int)(i & 1), b->blocks_pair, b->blocks_single, b->stream));
     if (todo & 1)
         for (plb_solve* s : b->solves) s->cur = 1 - s->cur;
     // a member's own calls (fields, conservation, steps) run on its stream:

@@ -182,12 +182,15 @@ struct BatchDomain {
 // One launch advances every domain by one step, reading f[parity] and
 // writing f[parity ^ 1]; `blocks` resident blocks walk the task list.
 // `moving`: some member has a moving wall.
-// `pairs`: the task list holds 64-node pair tasks (task .w = 1, domains with
-// even nx: the two-node pair kernel's work) beside 32-node one-node tasks.
-int nat_batch_step(int q, int storage, int arith, bool moving, bool pairs, const BatchDomain* doms,
-                   const int4* tiles, int ntiles, int parity, int blocks, cudaStream_t st);
-// Resident blocks per SM of the batch kernel (for sizing the grid).
-int nat_batch_blocks_per_sm(int q, int storage, int arith, bool moving, bool pairs);
+// The first npair tasks are 64-node pair tasks (task .w = 1, domains with
+// even nx: the two-node pair kernel's work), the rest 32-node one-node tasks;
+// each kind runs in its own kernel, on blocks_pair / blocks_single resident
+// blocks.
+int nat_batch_step(int q, int storage, int arith, bool moving, const BatchDomain* doms, const int4* tiles,
+                   int ntiles, int npair, int parity, int blocks_pair, int blocks_single, cudaStream_t st);
+// Resident blocks per SM of a batch kernel (for sizing the grid); kind 0:
+// one-node tasks, 1: pair tasks, 2: both in one kernel.
+int nat_batch_blocks_per_sm(int q, int storage, int arith, bool moving, int kind);
 constexpr int kBatchTile = 128;
 // The multi-step batch kernel's grid barrier (device memory; count and error
 // start at 0; error becomes 1 when a barrier's wait ran out).
@@ -212,9 +215,9 @@ int nat_collide_raw_trt(int q, int storage, bool has_mask, const Geo& g, const C
 int nat_aa_step_trt(int kind, int q, int storage, bool has_mask, const Geo& g, const CollideParams& cp,
                     const NativeParams& np, void* A, const float* rho, const float* u, const uint8_t* types,
                     cudaStream_t st);
-int nat_batch_blocks_per_sm_trt(int q, int storage, bool moving, bool pairs);
-int nat_batch_step_trt(int q, int storage, bool moving, bool pairs, const BatchDomain* doms, const int4* tiles,
-                       int ntiles, int parity, int blocks, cudaStream_t st);
+int nat_batch_blocks_per_sm_trt(int q, int storage, bool moving, int kind);
+int nat_batch_step_trt(int q, int storage, bool moving, const BatchDomain* doms, const int4* tiles, int ntiles,
+                       int npair, int parity, int blocks_pair, int blocks_single, cudaStream_t st);
 int nat_batch_step_multi_trt(int q, int storage, bool moving, bool pairs, const BatchDomain* doms,
                              const int4* tiles, int ntiles, int parity, int nsteps, int blocks, BatchSync* bs,
                              cudaStream_t st);

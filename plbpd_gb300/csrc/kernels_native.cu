@@ -190,16 +190,18 @@ int nat_aa_gather(int q, int storage, bool has_mask, bool swapped, const Geo& g,
 #undef CALL
 }
 
-int nat_batch_blocks_per_sm(int q, int storage, int arith, bool moving, bool pairs) {
-    if (arith == kArithTRT) return nat_batch_blocks_per_sm_trt(q, storage, moving, pairs);
-    return batch_blocks_per_sm<false>(q, storage, arith, moving, pairs);
+int nat_batch_blocks_per_sm(int q, int storage, int arith, bool moving, int kind) {
+    if (arith == kArithTRT) return nat_batch_blocks_per_sm_trt(q, storage, moving, kind);
+    return batch_blocks_per_sm<false>(q, storage, arith, moving, kind);
 }
 
-int nat_batch_step(int q, int storage, int arith, bool moving, bool pairs, const BatchDomain* doms,
-                   const int4* tiles, int ntiles, int parity, int blocks, cudaStream_t st) {
+int nat_batch_step(int q, int storage, int arith, bool moving, const BatchDomain* doms, const int4* tiles,
+                   int ntiles, int npair, int parity, int blocks_pair, int blocks_single, cudaStream_t st) {
     if (arith == kArithTRT)
-        return nat_batch_step_trt(q, storage, moving, pairs, doms, tiles, ntiles, parity, blocks, st);
-    return batch_step<false>(q, storage, arith, moving, pairs, doms, tiles, ntiles, parity, blocks, st);
+        return nat_batch_step_trt(q, storage, moving, doms, tiles, ntiles, npair, parity, blocks_pair, blocks_single,
+                                  st);
+    return batch_step<false>(q, storage, arith, moving, doms, tiles, ntiles, npair, parity, blocks_pair,
+                             blocks_single, st);
 }
 
 int nat_batch_step_multi(int q, int storage, int arith, bool moving, bool pairs, const BatchDomain* doms,

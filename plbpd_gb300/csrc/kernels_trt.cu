@@ -27,13 +27,14 @@ int nat_aa_step_trt(int kind, int q, int storage, bool has_mask, const Geo& g, c
 #undef CALL
 }
 
-int nat_batch_blocks_per_sm_trt(int q, int storage, bool moving, bool pairs) {
-    return batch_blocks_per_sm<true>(q, storage, kArithTRT, moving, pairs);
+int nat_batch_blocks_per_sm_trt(int q, int storage, bool moving, int kind) {
+    return batch_blocks_per_sm<true>(q, storage, kArithTRT, moving, kind);
 }
 
-int nat_batch_step_trt(int q, int storage, bool moving, bool pairs, const BatchDomain* doms, const int4* tiles,
-                       int ntiles, int parity, int blocks, cudaStream_t st) {
-    return batch_step<true>(q, storage, kArithTRT, moving, pairs, doms, tiles, ntiles, parity, blocks, st);
+int nat_batch_step_trt(int q, int storage, bool moving, const BatchDomain* doms, const int4* tiles, int ntiles,
+                       int npair, int parity, int blocks_pair, int blocks_single, cudaStream_t st) {
+    return batch_step<true>(q, storage, kArithTRT, moving, doms, tiles, ntiles, npair, parity, blocks_pair,
+                            blocks_single, st);
 }
 
 int nat_batch_step_multi_trt(int q, int storage, bool moving, bool pairs, const BatchDomain* doms,

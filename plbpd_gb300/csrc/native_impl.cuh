@@ -767,7 +767,7 @@ nat_fused_k(Geo g, CollideParams cp, NativeParams np, const typename Store<ST>::
 // The same two-node scheme serves FP32 and FP32-deviation storage (ST 0 and
 // 3: one aligned float2 a lane and direction), where it halves the
 // instructions a node takes and doubles the bytes a thread has in flight.
-template <int Q, bool MASK, bool MOVING, int ARITH, int FORM = 0, int ST = 1, bool CG = false>
+template <int Q, bool MASK, bool MOVING, int ARITH, int FORM = 0, int ST = 1, bool CG = false, bool VOTE = false>
 __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, const NativeParams& np,
                                         const typename Store<ST>::T* __restrict__ src,
                                         typename Store<ST>::T* __restrict__ dst, const uint8_t* __restrict__ types,
@@ -805,6 +805,12 @@ __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, c
         L0 = (t0 & kNearSolid) ? lw.x : 0u;
         L1 = (t1 & kNearSolid) ? lw.y : 0u;
     }
+    // batch tasks: a warp of solid pairs (a wall plane or row of a small
+    // domain, an obstacle's inside) needs no loads.  Not in the fused kernels:
+    // there the vote makes every warp's population loads wait for its type
+    // loads (D3Q27 duct with spheres, FP16: 40.5k -> 36.5k MLUPS), while
+    // wall rows are few; a batch of small walled domains gained 4 %.
+    if (MASK && VOTE && __all_sync(kFull, skip)) return;
     float2 f[Q];   // .x node x0, .y node x0 + 1
 #pragma unroll
     for (int k = 0; k < Q; ++k) {
@@ -1136,29 +1142,45 @@ nat_gather_k(Geo g, NativeParams np, const typename Store<ST>::T* __restrict__ s
 // so each lane forms its own row offsets.  A task's kind is the same for the
 // whole warp.  FP16 pairs use the paired update (form 0), FP32 storages the
 // scalar update of each node (form 2), which serves every arithmetic.
+//
+// KIND: the tasks a kernel runs.  A step launches one kernel for the pair
+// tasks and one for the 32-node tasks (the host puts the pair tasks first):
+// each kernel then holds only its own path's registers (D3Q19 FP32: 126
+// registers for both paths in one kernel).  The multi-step kernel runs both
+// kinds in one launch (kBatchMixed; .w says which).
+enum BatchKind : int { kBatchSingles = 0, kBatchPairs = 1, kBatchMixed = 2 };
+
 // The tasks of one step, walked by every resident warp (CG: L2-coherent
 // population loads, for the multi-step kernel).
-template <int Q, int ST, int ARITH, bool MOVING, bool PAIRS, bool CG>
+template <int Q, int ST, int ARITH, bool MOVING, int KIND, bool CG>
 __device__ __forceinline__ void batch_tasks(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks,
                                             int ntasks, int parity) {
     using T = typename Store<ST>::T;
     using R = typename Store<ST>::R;
     const int lane = threadIdx.x & 31;
     const int warps = gridDim.x * (kBatchTile / 32);
-    for (int t = blockIdx.x * (kBatchTile / 32) + (threadIdx.x >> 5); t < ntasks; t += warps) {
-        const int4 tk = __ldg(tasks + t);
+    // the next task's descriptor is loaded while this one runs, so a task
+    // does not start with a round trip for its own descriptor
+    const int t0 = blockIdx.x * (kBatchTile / 32) + (threadIdx.x >> 5);
+    int4 next = t0 < ntasks ? __ldg(tasks + t0) : make_int4(0, 0, 0, 0);
+    for (int t = t0; t < ntasks; t += warps) {
+        const int4 tk = next;
+        if (t + warps < ntasks) next = __ldg(tasks + t + warps);
         const BatchDomain& D = doms[tk.x];
         const Geo g = D.g;
-        if (PAIRS && tk.w) {
-            const int i = tk.z + 2 * lane;
-            const bool active = i < g.nx * g.ny;
-            const int y = active ? (int)((unsigned)i / (unsigned)g.nx) : 0;
-            const int x0 = active ? i - y * g.nx : 0;
-            h2_pair<Q, true, MOVING, ARITH, ST == 1 ? 0 : 2, ST, CG>(g, D.cp, D.np, static_cast<const T*>(D.f[parity]),
-                                                                    static_cast<T*>(D.f[parity ^ 1]), D.types, lane,
-                                                                    x0, y, tk.y, active);
-            continue;
+        if constexpr (KIND != kBatchSingles) {
+            if (KIND == kBatchPairs || tk.w) {
+                const int i = tk.z + 2 * lane;
+                const bool active = i < g.nx * g.ny;
+                const int y = active ? (int)((unsigned)i / (unsigned)g.nx) : 0;
+                const int x0 = active ? i - y * g.nx : 0;
+                h2_pair<Q, true, MOVING, ARITH, ST == 1 ? 0 : 2, ST, CG, true>(
+                    g, D.cp, D.np, static_cast<const T*>(D.f[parity]), static_cast<T*>(D.f[parity ^ 1]), D.types,
+                    lane, x0, y, tk.y, active);
+                continue;
+            }
         }
+        if constexpr (KIND == kBatchPairs) continue;
         // 32 consecutive nodes of the plane z (flattened y * nx + x), so short
         // rows do not leave lanes idle
         const int i = tk.z + lane;
@@ -1187,12 +1209,15 @@ __device__ __forceinline__ void batch_tasks(const BatchDomain* __restrict__ doms
 }
 
 // FP16 batches of D2Q9/D3Q19 at six blocks an SM (at most 80 registers):
-// config 4's FP16 batch 33.6k -> 36.0k MLUPS; FP32 storages spill under the
-// cap and keep the compiler's choice.
-template <int Q, int ST, int ARITH, bool MOVING, bool PAIRS = false>
-__global__ void __launch_bounds__(kBatchTile, (ST == 1 && Q <= 19) ? 6 : 1)
+// config 4's FP16 batch 33.6k -> 36.0k MLUPS.  FP32 storages, the most
+// blocks an SM without spills: pair tasks five (D2Q9/D3Q19, 96 registers)
+// and four (D3Q27, 128), one-node tasks six (D2Q9/D3Q19, 80); the
+// compiler's choices were 122, 156 and 96.  These kernels are latency-bound
+// (long-scoreboard stalls, ~31 % warps active at 96 registers).
+template <int Q, int ST, int ARITH, bool MOVING, int KIND>
+__global__ void __launch_bounds__(kBatchTile, (ST == 1 && Q <= 19) ? 6 : (KIND == kBatchPairs ? (Q <= 19 ? 5 : 4) : (Q <= 19 ? 6 : 1)))
 nat_batch_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks, int ntasks, int parity) {
-    batch_tasks<Q, ST, ARITH, MOVING, PAIRS, false>(doms, tasks, ntasks, parity);
+    batch_tasks<Q, ST, ARITH, MOVING, KIND, false>(doms, tasks, ntasks, parity);
 }
 
 // ---------------------------------------------------------------------------
@@ -1241,7 +1266,8 @@ __global__ void __launch_bounds__(kBatchTile)
 nat_batch_multi_k(const BatchDomain* __restrict__ doms, const int4* __restrict__ tasks, int ntasks, int parity,
                   int nsteps, BatchSync* bs) {
     for (int s = 0; s < nsteps; ++s) {
-        batch_tasks<Q, ST, ARITH, MOVING, PAIRS, true>(doms, tasks, ntasks, parity ^ (s & 1));
+        batch_tasks<Q, ST, ARITH, MOVING, PAIRS ? kBatchMixed : kBatchSingles, true>(doms, tasks, ntasks,
+                                                                                   parity ^ (s & 1));
         if (s + 1 < nsteps && !batch_grid_sync(bs, gridDim.x)) return;
     }
 }
@@ -1458,57 +1484,68 @@ int aa_q(int kind, int storage, int arith, bool m, const Geo& g, const CollidePa
     });
 }
 
-// Batches hold FP32, FP32-deviation or FP16 storage; `pairs`: the task list
-// holds 64-node pair tasks (domains with even nx) beside 32-node ones.
+// Batches hold FP32, FP32-deviation or FP16 storage; kind: the BatchKind of
+// the one-step kernel.
 template <bool TRT, bool MV>
-const void* batch_kernel_for(int q, int storage, int arith, bool pairs) {
+const void* batch_kernel_for(int q, int storage, int arith, int kind) {
     if (storage == 2) return nullptr;
     const void* k = nullptr;
     with_storage_arith<TRT>(storage, arith, [&](auto stc, auto arc) {
         constexpr int ST = decltype(stc)::value == 2 ? 0 : decltype(stc)::value, AR = decltype(arc)::value;
-        if (pairs)
-            k = q == 9 ? (const void*)nat_batch_k<9, ST, AR, MV, true>
-              : q == 19 ? (const void*)nat_batch_k<19, ST, AR, MV, true>
-              : q == 27 ? (const void*)nat_batch_k<27, ST, AR, MV, true> : nullptr;
-        else
-            k = q == 9 ? (const void*)nat_batch_k<9, ST, AR, MV>
-              : q == 19 ? (const void*)nat_batch_k<19, ST, AR, MV>
-              : q == 27 ? (const void*)nat_batch_k<27, ST, AR, MV> : nullptr;
+        auto pick = [&](auto kc) {
+            constexpr int K = decltype(kc)::value;
+            k = q == 9 ? (const void*)nat_batch_k<9, ST, AR, MV, K>
+              : q == 19 ? (const void*)nat_batch_k<19, ST, AR, MV, K>
+              : q == 27 ? (const void*)nat_batch_k<27, ST, AR, MV, K> : nullptr;
+        };
+        if (kind == kBatchPairs) pick(IC<kBatchPairs>{});
+        else if (kind == kBatchMixed) pick(IC<kBatchMixed>{});
+        else pick(IC<kBatchSingles>{});
         return 0;
     });
     return k;
 }
 
 template <bool TRT>
-int batch_blocks_per_sm(int q, int storage, int arith, bool moving, bool pairs) {
-    const void* k = moving ? batch_kernel_for<TRT, true>(q, storage, arith, pairs)
-                           : batch_kernel_for<TRT, false>(q, storage, arith, pairs);
+int batch_blocks_per_sm(int q, int storage, int arith, bool moving, int kind) {
+    const void* k = moving ? batch_kernel_for<TRT, true>(q, storage, arith, kind)
+                           : batch_kernel_for<TRT, false>(q, storage, arith, kind);
     if (!k) return 0;
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kBatchTile, 0) != cudaSuccess) return 0;
     return n;
 }
 
+// One step: the pair tasks tiles[0, npair) and the 32-node tasks
+// tiles[npair, ntiles), each kind in its own kernel on `st` (at most
+// blocks_pair / blocks_single resident blocks, one task per warp).
 template <bool TRT>
-int batch_step(int q, int storage, int arith, bool moving, bool pairs, const BatchDomain* doms, const int4* tiles,
-               int ntiles, int parity, int blocks, cudaStream_t st) {
+int batch_step(int q, int storage, int arith, bool moving, const BatchDomain* doms, const int4* tiles, int ntiles,
+               int npair, int parity, int blocks_pair, int blocks_single, cudaStream_t st) {
     if (ntiles <= 0) return 0;
     if (storage == 2) return (int)cudaErrorInvalidValue;
-    const int need = (ntiles + kBatchTile / 32 - 1) / (kBatchTile / 32);   // one task per warp
-    if (blocks > need) blocks = need;
+    auto grid = [](int tasks, int blocks) {
+        const int need = (tasks + kBatchTile / 32 - 1) / (kBatchTile / 32);
+        return blocks < need ? (blocks > 0 ? blocks : 1) : need;
+    };
     return with_storage_arith<TRT>(storage, arith, [&](auto stc, auto arc) {
         constexpr int ST = decltype(stc)::value == 2 ? 0 : decltype(stc)::value, AR = decltype(arc)::value;
         auto go = [&](auto qc) {
             constexpr int Q = decltype(qc)::value;
-            if (pairs) {
-                if (moving)
-                    nat_batch_k<Q, ST, AR, true, true><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);
-                else
-                    nat_batch_k<Q, ST, AR, false, true><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);
-                return (int)cudaGetLastError();
+            if (npair > 0) {
+                const int gb = grid(npair, blocks_pair);
+                if (moving) nat_batch_k<Q, ST, AR, true, kBatchPairs><<<gb, kBatchTile, 0, st>>>(doms, tiles, npair, parity);
+                else nat_batch_k<Q, ST, AR, false, kBatchPairs><<<gb, kBatchTile, 0, st>>>(doms, tiles, npair, parity);
+                const cudaError_t e = cudaGetLastError();
+                if (e != cudaSuccess) return (int)e;
             }
-            if (moving) nat_batch_k<Q, ST, AR, true><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);
-            else nat_batch_k<Q, ST, AR, false><<<blocks, kBatchTile, 0, st>>>(doms, tiles, ntiles, parity);
+            const int ns = ntiles - npair;
+            if (ns > 0) {
+                const int gb = grid(ns, blocks_single);
+                const int4* t1 = tiles + npair;
+                if (moving) nat_batch_k<Q, ST, AR, true, kBatchSingles><<<gb, kBatchTile, 0, st>>>(doms, t1, ns, parity);
+                else nat_batch_k<Q, ST, AR, false, kBatchSingles><<<gb, kBatchTile, 0, st>>>(doms, t1, ns, parity);
+            }
             return (int)cudaGetLastError();
         };
         return q == 9 ? go(IC<9>{}) : q == 19 ? go(IC<19>{}) : q == 27 ? go(IC<27>{}) : (int)cudaErrorInvalidValue;
