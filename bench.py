@@ -22,7 +22,8 @@ barriers, and the slowest rank's time is used.
              L2, so no flush is needed between steps.
   e2e        MLUPS through the C ABI with host buffers: upload n, rho, u from
              pinned memory (plbpd's layout), march K steps, read rho and u back;
-             with the achieved host-to-device and device-to-host rates.
+             with the achieved host-to-device and device-to-host rates (after
+             one untimed pass that loads the layout kernels).
   roofline   achieved = 152 B/cell (19 populations read and written, FP32) x
              cells / mean duration of one fused-kernel launch, against the
              measured HBM copy bandwidth; traffic = the kernel's DRAM bytes per
@@ -378,6 +379,12 @@ def run_gpu_arm(args):
     kms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
 
     # ---- e2e through the C ABI with host buffers -------------------------------
+    # one untimed pass first: the layout and read-back kernels load on their
+    # first launch (lazy module loading), which took 30 ms of a 40 ms pass
+    upload()
+    s.step(min(args.steps, 64))
+    s.get(capi.FIELD_RHO, out_rho.array)
+    s.get(capi.FIELD_U, out_u.array)
     e2e_iters = max(1, args.e2e_iters)
     barrier(dist, local)
     torch.cuda.synchronize()
@@ -426,7 +433,7 @@ def run_gpu_arm(args):
                    "boundaries": "periodic x/y/z", "storage": args.storage, "semantics": "native",
                    "arithmetic": ARITHS[args.arith][1],
                    "l2": "no flush: populations 2.7 GB > 129 MB L2", "parallelism": f"replicas x{world}",
-                   "e2e": f"{e2e_iters} x (upload n/rho/u, {args.steps} steps, read rho/u)"},
+                   "e2e": f"{e2e_iters} x (upload n/rho/u, {args.steps} steps, read rho/u) after one untimed pass"},
         "e2e": {"value": round(e2e_val, 1), "unit": "MLUPS", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
                 "h2d_gbs": round(up_bytes * e2e_iters / t_up / 1e9, 1),

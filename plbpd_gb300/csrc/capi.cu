@@ -1145,8 +1145,14 @@ int enqueue_get_field(plb_solve* s, int32_t which, float* out, bool gathered, si
                                          s->rho, s->u, s->types, s->stream));
             }
         } else if (s->post) {
-            if (!gathered || which == PLB_FIELD_N) PLB_TRY(nat_gather_to_other(s));
-            n_buf = 1 - s->cur;
+            if (which == PLB_FIELD_N) {
+                PLB_TRY(nat_gather_to_other(s));
+                n_buf = 1 - s->cur;
+            } else if (!gathered) {
+                // rho and u only: the gather writes no populations
+                PLB_KERNEL(nat_gather(s->q, s->storage, s->has_mask, s->g, s->np, s->f[s->cur], nullptr, s->rho,
+                                      s->u, s->types, s->stream));
+            }
         }
     } else if (which == PLB_FIELD_RHO || which == PLB_FIELD_U) {
         PLB_TRY(ref_materialize_fields(s));
