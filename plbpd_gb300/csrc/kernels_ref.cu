@@ -12,6 +12,9 @@
 // The ρ field is written only where the no-slip rule reads it, and the
 // moments are computed again by the next step, so the only per-cell traffic
 // is one read and one write of each population.
+#include <cstdlib>
+#include <cstring>
+
 #include "engine.h"
 #include "ref_ops.cuh"
 
@@ -21,22 +24,15 @@ namespace {
 constexpr int kBlockX = 128;
 
 // ---------------------------------------------------------------------------
+// One node's work before the push: its moments (or, on a march's first step,
+// the fields as the caller left them), the resets, the density the no-slip
+// rule of this step reads, and the collision in place.
 template <int Q, int ARITH, bool FIRST>
-__global__ void __launch_bounds__(kBlockX)
-ref_fused_step_k(Geo g, CollideParams cp, FaceParams fp, float* __restrict__ cur,
-                 float* __restrict__ nxt, float* __restrict__ rho_f, const float* __restrict__ u_f,
-                 int wb_all) {
-    const int x = blockIdx.x * kBlockX + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
-    if (x >= g.nx) return;
-    const long long node = g.idx(x, y, z);
-    float f[Q];
-#pragma unroll
-    for (int k = 0; k < Q; ++k) f[k] = cur[k * g.ks + node];
-
+__device__ __forceinline__ void ref_node_update(const Geo& g, const CollideParams& cp, const FaceParams& fp,
+                                                float* __restrict__ rho_f, const float* __restrict__ u_f, int x,
+                                                int y, int z, long long node, float (&f)[Q]) {
     float rho, ux, uy, uz;
     if (FIRST) {
-        // first step of a march: the fields as the caller left them
         rho = rho_f[node];
         ux = u_f[node]; uy = u_f[g.ks + node]; uz = u_f[2 * g.ks + node];
     } else {
@@ -48,22 +44,112 @@ ref_fused_step_k(Geo g, CollideParams cp, FaceParams fp, float* __restrict__ cur
 #pragma unroll
     for (int fc = 0; fc < 6; ++fc) near |= ((fp.noslip_mask >> fc) & 1) && near_face(fc, x, y, z, g);
     if (near && !FIRST) rho_f[node] = rho;
-
     collide_node<Q, ARITH>(f, rho, ux, uy, uz, cp);
+}
 
+// plbpd collides in place, so a slot that the next push leaves unwritten
+// still holds this step's collided value; only boundary-layer nodes own such
+// slots (D2Q9 never moves along y, so its y faces own none).  The last step
+// of a march writes every node back, which leaves the other buffer exactly as
+// plbpd's ntmp.
+template <int Q>
+__device__ __forceinline__ bool ref_outer(const Geo& g, int x, int y, int z) {
+    return x == 0 || x == g.nx - 1 || z == 0 || z == g.nz - 1 || (Q != 9 && (y == 0 || y == g.ny - 1));
+}
+
+template <int Q, int ARITH, bool FIRST>
+__global__ void __launch_bounds__(kBlockX, (Q == 19 && ARITH != kArithReference) ? 6 : 0)
+ref_fused_step_k(Geo g, CollideParams cp, FaceParams fp, float* __restrict__ cur,
+                 float* __restrict__ nxt, float* __restrict__ rho_f, const float* __restrict__ u_f,
+                 int wb_all) {
+    const int x = blockIdx.x * kBlockX + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= g.nx) return;
+    const long long node = g.idx(x, y, z);
+    float f[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) f[k] = cur[k * g.ks + node];
+    ref_node_update<Q, ARITH, FIRST>(g, cp, fp, rho_f, u_f, x, y, z, node, f);
 #pragma unroll
     for (int k = 0; k < Q; ++k) nxt[k * g.ks + node + push_offset<Q>(k, g)] = f[k];
-
-    // plbpd collides in place, so a slot that the next push leaves unwritten
-    // still holds this step's collided value; only boundary-layer nodes own
-    // such slots (D2Q9 never moves along y, so its y faces own none).  The
-    // last step of a march writes every node back, which leaves the other
-    // buffer exactly as plbpd's ntmp.
-    const bool outer = x == 0 || x == g.nx - 1 || z == 0 || z == g.nz - 1 ||
-                       (Q != 9 && (y == 0 || y == g.ny - 1));
-    if (outer || wb_all) {
+    if (ref_outer<Q>(g, x, y, z) || wb_all) {
 #pragma unroll
         for (int k = 0; k < Q; ++k) cur[k * g.ks + node] = f[k];
+    }
+}
+
+// The same step for two neighbouring nodes (x0, x0 + 1) a thread, nx even
+// and x0 even: a row starts at element offset 8 and has a pitch of a
+// multiple of 8, so every pair is an aligned float2, loaded in one access.
+// Each node's update is ref_node_update, so the values are those of the
+// one-node kernel.  The push of direction k moves the pair by c_k; along y
+// and z that is another row, along x it is one element, so the stores are
+// realigned through the neighbouring lanes: for c_x = +1 the pair slot
+// (x0, x0 + 1) receives (the previous lane's x0 - 1, this lane's x0), for
+// c_x = -1 (this lane's x0 + 1, the next lane's x0 + 2).  A slot whose source
+// is in another warp or outside the row is stored alone by the lane that
+// holds its source, and a slot whose source is a halo node is not stored at
+// all -- exactly the slots the one-node kernel writes, each written once.
+template <int Q, int ARITH, bool FIRST, int BX>
+__global__ void __launch_bounds__(BX)
+ref_fused_pair_k(Geo g, CollideParams cp, FaceParams fp, float* __restrict__ cur, float* __restrict__ nxt,
+                 float* __restrict__ rho_f, const float* __restrict__ u_f, int wb_all) {
+    const unsigned kFull = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int x0 = 2 * (blockIdx.x * BX + threadIdx.x);
+    const int y = blockIdx.y, z = blockIdx.z;
+    const bool active = x0 < g.nx;
+    const long long node0 = g.idx(active ? x0 : 0, y, z);
+    float a[Q], b[Q];   // nodes x0 and x0 + 1
+    if (active) {
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            const float2 v = *reinterpret_cast<const float2*>(cur + k * g.ks + node0);
+            a[k] = v.x;
+            b[k] = v.y;
+        }
+        ref_node_update<Q, ARITH, FIRST>(g, cp, fp, rho_f, u_f, x0, y, z, node0, a);
+        ref_node_update<Q, ARITH, FIRST>(g, cp, fp, rho_f, u_f, x0 + 1, y, z, node0 + 1, b);
+    } else {
+#pragma unroll
+        for (int k = 0; k < Q; ++k) a[k] = b[k] = 0.0f;
+    }
+    const bool lo_edge = lane == 0 || x0 == 0;           // x0 - 1 is not the previous lane's
+    const bool hi_edge = lane == 31 || x0 + 2 >= g.nx;   // x0 + 2 is not the next lane's
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        const int cx = Lattice<Q>::cx(k);
+        float* d = nxt + k * g.ks + node0 + (long long)Lattice<Q>::cy(k) * g.ys +
+                   (long long)Lattice<Q>::cz(k) * g.zs;   // slot x0 of the destination row
+        if (cx == 0) {
+            if (active) *reinterpret_cast<float2*>(d) = make_float2(a[k], b[k]);
+        } else if (cx > 0) {
+            const float pb = __shfl_up_sync(kFull, b[k], 1);
+            if (active) {
+                if (!lo_edge) *reinterpret_cast<float2*>(d) = make_float2(pb, a[k]);
+                else d[1] = a[k];
+                if (hi_edge) d[2] = b[k];
+            }
+        } else {
+            const float na = __shfl_down_sync(kFull, a[k], 1);
+            if (active) {
+                if (!hi_edge) *reinterpret_cast<float2*>(d) = make_float2(b[k], na);
+                else d[0] = b[k];
+                if (lo_edge) d[-1] = a[k];
+            }
+        }
+    }
+    if (active) {
+        const bool oa = ref_outer<Q>(g, x0, y, z) || wb_all, ob = ref_outer<Q>(g, x0 + 1, y, z) || wb_all;
+        if (oa || ob) {
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                float* c = cur + k * g.ks + node0;
+                if (oa && ob) *reinterpret_cast<float2*>(c) = make_float2(a[k], b[k]);
+                else if (oa) c[0] = a[k];
+                else c[1] = b[k];
+            }
+        }
     }
 }
 
@@ -217,11 +303,45 @@ ref_reset_k(Geo g, FaceParams fp, int velocity, int density, float* __restrict__
 
 dim3 cell_grid(const Geo& g) { return dim3((g.nx + kBlockX - 1) / kBlockX, g.ny, g.nz); }
 
+// Which form of the step runs (nx even for the pair form).  Measured on
+// 256^3 / 192^3 / 2048^2 channels: D2Q9 47.8k -> 56.6k MLUPS and D3Q27 16.4k
+// -> 17.4k with the pair form; D3Q19 31.5k (plbpd's arithmetic, 72 registers)
+// and 31.5k (FP32 arithmetic, capped at 80 registers) with the one-node form,
+// 28.3k / 30.8k with the pair form.  PLB_REF_PAIR=1 takes the pair form
+// whenever nx is even, PLB_REF_PAIR=0 never.
+bool ref_use_pair(int q, int nx) {
+    if (nx % 2 != 0) return false;
+    const char* e = std::getenv("PLB_REF_PAIR");
+    if (e && std::strcmp(e, "0") == 0) return false;
+    if (e && std::strcmp(e, "1") == 0) return true;
+    return q != 19;
+}
+
+template <int Q, int ARITH>
+int launch_ref_pair(bool first, const Geo& g, const CollideParams& cp, const FaceParams& fp, float* cur, float* nxt,
+                    float* rho, float* u, int wb, cudaStream_t st) {
+    auto go = [&](auto bxc) {
+        constexpr int BX = decltype(bxc)::value;
+        const dim3 grid((unsigned)((g.nx + 2 * BX - 1) / (2 * BX)), (unsigned)g.ny, (unsigned)g.nz);
+        if (first) ref_fused_pair_k<Q, ARITH, true, BX><<<grid, BX, 0, st>>>(g, cp, fp, cur, nxt, rho, u, wb);
+        else ref_fused_pair_k<Q, ARITH, false, BX><<<grid, BX, 0, st>>>(g, cp, fp, cur, nxt, rho, u, wb);
+    };
+    // whole 128-thread blocks when the row is a whole number of them, else one warp a block
+    if (g.nx % (2 * kBlockX) == 0) go(std::integral_constant<int, kBlockX>{});
+    else go(std::integral_constant<int, 32>{});
+    return (int)cudaGetLastError();
+}
+
 template <int Q>
 int fused_dispatch(int arith, bool first, bool wb_all, const Geo& g, const CollideParams& cp,
                    const FaceParams& fp, float* cur, float* nxt, float* rho, float* u, cudaStream_t st) {
     const dim3 grid = cell_grid(g);
     const int wb = wb_all ? 1 : 0;
+    if (ref_use_pair(Q, g.nx)) {
+        if (arith == kArithReference) return launch_ref_pair<Q, kArithReference>(first, g, cp, fp, cur, nxt, rho, u, wb, st);
+        if (arith == kArithTRT) return launch_ref_pair<Q, kArithTRT>(first, g, cp, fp, cur, nxt, rho, u, wb, st);
+        return launch_ref_pair<Q, kArithFP32>(first, g, cp, fp, cur, nxt, rho, u, wb, st);
+    }
     if (arith == kArithReference) {
         if (first) ref_fused_step_k<Q, kArithReference, true><<<grid, kBlockX, 0, st>>>(g, cp, fp, cur, nxt, rho, u, wb);
         else ref_fused_step_k<Q, kArithReference, false><<<grid, kBlockX, 0, st>>>(g, cp, fp, cur, nxt, rho, u, wb);

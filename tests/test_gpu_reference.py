@@ -20,8 +20,13 @@ def gpu_solve(cfg, arith=None, semantics=None):
                              arith=capi.ARITH_REFERENCE if arith is None else arith)
 
 
+@pytest.mark.parametrize("pair", ["1", "0"])
 @pytest.mark.parametrize("case", sorted(CASES))
-def test_steps_match_reference(case):
+def test_steps_match_reference(case, pair, monkeypatch):
+    """Steps against the reference's own fields, the step in its two-node
+    form wherever nx is even (PLB_REF_PAIR=1) or in its one-node form
+    (PLB_REF_PAIR=0)."""
+    monkeypatch.setenv("PLB_REF_PAIR", pair)
     ref = load_npz(f"ref_{case}.npz")
     with gpu_solve(CASES[case]) as s:
         s.initialize()
@@ -76,13 +81,14 @@ def test_sourcemap_matches_reference(case):
         assert_bitexact(s.get(1), ref["ntmp"], "source map ntmp")
 
 
-@pytest.mark.parametrize("cluster", ["1", "0"])
-def test_channel_10000_steps_match_reference_digest(golden, monkeypatch, cluster):
+@pytest.mark.parametrize("cluster,pair", [("1", "1"), ("0", "1"), ("0", "0")])
+def test_channel_10000_steps_match_reference_digest(golden, monkeypatch, cluster, pair):
     """The 128 x 64 D2Q9 channel, 10,000 steps in one march: every byte of n,
     ntmp, rho and u equals the reference's -- with the march in one cluster
     launch (state in distributed shared memory) and with three launches a
-    step (PLB_REF_CLUSTER=0)."""
+    step (PLB_REF_CLUSTER=0), the step in its two-node or one-node form."""
     monkeypatch.setenv("PLB_REF_CLUSTER", cluster)
+    monkeypatch.setenv("PLB_REF_PAIR", pair)
     with gpu_solve(CHANNEL) as s:
         s.initialize()
         s.step(10000)
@@ -105,9 +111,11 @@ def test_long_march_uses_graphs_and_matches_oracle(case):
             assert_bitexact(s.get(w), p.get(w), f"{case} {k}")
 
 
+@pytest.mark.parametrize("pair", ["1", "0"])
 @pytest.mark.parametrize("case", sorted(CASES))
-def test_fp32_arith_matches_oracle(case):
+def test_fp32_arith_matches_oracle(case, pair, monkeypatch):
     """FP32-only collision arithmetic: bit-exact against the oracle's FP32 mode."""
+    monkeypatch.setenv("PLB_REF_PAIR", pair)
     from plbpd_gb300 import capi
     cfg = CASES[case]
     p = po.Port(**cfg, arith=po.ARITH_FP32)
@@ -175,3 +183,25 @@ def test_cluster_march_equals_three_launch_path(case, split, monkeypatch):
             out[cluster] = [s.get(w) for _, w in FIELDS]
     for (k, _), a, b in zip(FIELDS, out["1"], out["0"]):
         assert_bitexact(a, b, f"{case} {split} {k}")
+
+
+@pytest.mark.parametrize("case,dims", [("d3q19_xy_periodic", (130, 5, 4)), ("d3q27_duct", (256, 3, 4)),
+                                       ("d3q19_thin_walls", (66, 3, 3))])
+def test_pair_step_with_wide_rows(case, dims, monkeypatch):
+    """Rows of several warps (and of 128-thread blocks at 256): the two-node
+    step's stores across warp and block edges, and at the row's halo ends,
+    give the oracle's fields, and the one-node step's."""
+    cfg = dict(CASES[case], nx=dims[0], ny=dims[1], nz=dims[2])
+    p = po.Port(**cfg)
+    p.initialize()
+    p.step(9)
+    out = {}
+    for pair in ("1", "0"):
+        monkeypatch.setenv("PLB_REF_PAIR", pair)
+        with gpu_solve(cfg) as s:
+            s.initialize()
+            s.step(9)
+            out[pair] = [s.get(w) for _, w in FIELDS]
+    for (k, w), a, b in zip(FIELDS, out["1"], out["0"]):
+        assert_bitexact(a, p.get(w), f"{case} {dims} {k} pair")
+        assert_bitexact(b, p.get(w), f"{case} {dims} {k} one-node")
