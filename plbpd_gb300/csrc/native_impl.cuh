@@ -671,6 +671,19 @@ __device__ __forceinline__ void rest_state(typename Store<ST>::R (&f)[Q], typena
     rho = R(1);
 }
 
+// A row load of the pair kernels through the read-only path with a 256-byte
+// L2 fill: the next warp of the row reads the other half of the block.
+__device__ __forceinline__ __half2 ld_row_h2(const __half2* p) {
+    unsigned int r;
+    asm("ld.global.nc.L2::256B.b32 %0, [%1];" : "=r"(r) : "l"(p));
+    return *reinterpret_cast<const __half2*>(&r);
+}
+__device__ __forceinline__ float2 ld_row_f2(const float2* p) {
+    float2 r;
+    asm("ld.global.nc.L2::256B.v2.f32 {%0, %1}, [%2];" : "=f"(r.x), "=f"(r.y) : "l"(p));
+    return r;
+}
+
 // The solid-link mask of a node (0 for nodes away from solids).
 template <bool MASK>
 __device__ __forceinline__ uint32_t links_of(const uint8_t t, const uint32_t* __restrict__ links, long long node) {
@@ -820,10 +833,10 @@ __device__ __forceinline__ void h2_pair(const Geo& g, const CollideParams& cp, c
         if (active) {
             if constexpr (ST == 1) {
                 const __half2* a = reinterpret_cast<const __half2*>(src + row + x0);
-                v = __half22float2(CG ? __ldcg(a) : __ldg(a));
+                v = __half22float2(CG ? __ldcg(a) : ld_row_h2(a));
             } else {
                 const float2* a = reinterpret_cast<const float2*>(src + row + x0);
-                v = CG ? __ldcg(a) : __ldg(a);
+                v = CG ? __ldcg(a) : ld_row_f2(a);
             }
         }
         if (cx == 0) {
