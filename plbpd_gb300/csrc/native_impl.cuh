@@ -98,6 +98,23 @@ __device__ __forceinline__ typename Store<ST>::R ld_pop(const typename Store<ST>
     else return __ldcg(p + i);
 }
 
+// A one-node kernel's pull of a whole row (the streaming loads): as ld_pop,
+// with 256-byte L2 fills as the pair kernels' row loads.
+template <int ST, bool CG>
+__device__ __forceinline__ typename Store<ST>::R ld_pull(const typename Store<ST>::T* p, long long i) {
+    if constexpr (CG || ST == 2) {
+        return ld_pop<ST, CG>(p, i);
+    } else if constexpr (ST == 1) {
+        unsigned short r;
+        asm("ld.global.nc.L2::256B.b16 %0, [%1];" : "=h"(r) : "l"(p + i));
+        return __half2float(__ushort_as_half(r));
+    } else {
+        float r;
+        asm("ld.global.nc.L2::256B.f32 %0, [%1];" : "=f"(r) : "l"(p + i));
+        return r;
+    }
+}
+
 // Neighbour index helper: element offsets of x-1, x, x+1 (and y, z) with the
 // periodic axes wrapped.  A fluid node never has a neighbour outside the box
 // along a walled axis, because the wall layer in between is solid, so kernels
@@ -699,7 +716,7 @@ template <int Q, int ST, bool CG = false>
 __device__ __forceinline__ void stream_loads(const typename Store<ST>::T* __restrict__ src, const Geo& g,
                                              const Nbr& nb, typename Store<ST>::R (&f)[Q]) {
 #pragma unroll
-    for (int k = 0; k < Q; ++k) f[k] = ld_pop<ST, CG>(src, k * g.ks + nb.at<Q>(k, -1));
+    for (int k = 0; k < Q; ++k) f[k] = ld_pull<ST, CG>(src, k * g.ks + nb.at<Q>(k, -1));
 }
 
 template <int Q, int ST, bool CG = false>
