@@ -24,6 +24,20 @@ namespace {
 constexpr int kBlockX = 128;
 
 // ---------------------------------------------------------------------------
+// A node's population loads, with 256-byte L2 fills (the next warp of the row
+// reads the other half).  Plain loads, not the read-only path: the step
+// writes boundary-layer nodes' own slots of the same buffer back.
+__device__ __forceinline__ float ld_row(const float* p) {
+    float r;
+    asm volatile("ld.global.L2::256B.f32 %0, [%1];" : "=f"(r) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ float2 ld_row2(const float* p) {
+    float2 r;
+    asm volatile("ld.global.L2::256B.v2.f32 {%0, %1}, [%2];" : "=f"(r.x), "=f"(r.y) : "l"(p));
+    return r;
+}
+
 // One node's work before the push: its moments (or, on a march's first step,
 // the fields as the caller left them), the resets, the density the no-slip
 // rule of this step reads, and the collision in place.
@@ -68,7 +82,7 @@ ref_fused_step_k(Geo g, CollideParams cp, FaceParams fp, float* __restrict__ cur
     const long long node = g.idx(x, y, z);
     float f[Q];
 #pragma unroll
-    for (int k = 0; k < Q; ++k) f[k] = cur[k * g.ks + node];
+    for (int k = 0; k < Q; ++k) f[k] = ld_row(cur + k * g.ks + node);
     ref_node_update<Q, ARITH, FIRST>(g, cp, fp, rho_f, u_f, x, y, z, node, f);
 #pragma unroll
     for (int k = 0; k < Q; ++k) nxt[k * g.ks + node + push_offset<Q>(k, g)] = f[k];
@@ -104,7 +118,7 @@ ref_fused_pair_k(Geo g, CollideParams cp, FaceParams fp, float* __restrict__ cur
     if (active) {
 #pragma unroll
         for (int k = 0; k < Q; ++k) {
-            const float2 v = *reinterpret_cast<const float2*>(cur + k * g.ks + node0);
+            const float2 v = ld_row2(cur + k * g.ks + node0);
             a[k] = v.x;
             b[k] = v.y;
         }
