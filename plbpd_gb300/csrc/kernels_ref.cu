@@ -317,18 +317,14 @@ ref_reset_k(Geo g, FaceParams fp, int velocity, int density, float* __restrict__
 
 dim3 cell_grid(const Geo& g) { return dim3((g.nx + kBlockX - 1) / kBlockX, g.ny, g.nz); }
 
-// Which form of the step runs (nx even for the pair form).  Measured on
-// 256^3 / 192^3 / 2048^2 channels: D2Q9 47.8k -> 56.6k MLUPS and D3Q27 16.4k
-// -> 17.4k with the pair form; D3Q19 31.5k (plbpd's arithmetic, 72 registers)
-// and 31.5k (FP32 arithmetic, capped at 80 registers) with the one-node form,
-// 28.3k / 30.8k with the pair form.  PLB_REF_PAIR=1 takes the pair form
-// whenever nx is even, PLB_REF_PAIR=0 never.
-bool ref_use_pair(int q, int nx) {
+// Which form of the step runs: the pair form whenever nx is even, unless
+// PLB_REF_PAIR=0.  Measured on 256^3 / 192^3 / 2048^2 channels with plbpd's
+// arithmetic, one-node against pair form: D3Q19 31.8k -> 33.7k MLUPS (FP32
+// arithmetic 31.7k -> 34.0k), D3Q27 16.4k -> 19.4k, D2Q9 51.9k -> 62.5k.
+bool ref_use_pair(int nx) {
     if (nx % 2 != 0) return false;
     const char* e = std::getenv("PLB_REF_PAIR");
-    if (e && std::strcmp(e, "0") == 0) return false;
-    if (e && std::strcmp(e, "1") == 0) return true;
-    return q != 19;
+    return !(e && std::strcmp(e, "0") == 0);
 }
 
 template <int Q, int ARITH>
@@ -351,7 +347,7 @@ int fused_dispatch(int arith, bool first, bool wb_all, const Geo& g, const Colli
                    const FaceParams& fp, float* cur, float* nxt, float* rho, float* u, cudaStream_t st) {
     const dim3 grid = cell_grid(g);
     const int wb = wb_all ? 1 : 0;
-    if (ref_use_pair(Q, g.nx)) {
+    if (ref_use_pair(g.nx)) {
         if (arith == kArithReference) return launch_ref_pair<Q, kArithReference>(first, g, cp, fp, cur, nxt, rho, u, wb, st);
         if (arith == kArithTRT) return launch_ref_pair<Q, kArithTRT>(first, g, cp, fp, cur, nxt, rho, u, wb, st);
         return launch_ref_pair<Q, kArithFP32>(first, g, cp, fp, cur, nxt, rho, u, wb, st);

@@ -24,7 +24,7 @@ def gpu_solve(cfg, arith=None, semantics=None):
 @pytest.mark.parametrize("case", sorted(CASES))
 def test_steps_match_reference(case, pair, monkeypatch):
     """Steps against the reference's own fields, the step in its two-node
-    form wherever nx is even (PLB_REF_PAIR=1) or in its one-node form
+    form wherever nx is even (the default) or in its one-node form
     (PLB_REF_PAIR=0)."""
     monkeypatch.setenv("PLB_REF_PAIR", pair)
     ref = load_npz(f"ref_{case}.npz")
