@@ -7,8 +7,8 @@ Workloads
             without a node-type mask)
   duct      NATIVE semantics, periodic x, no-slip walls on y and z, body force;
             --spheres adds the seeded random-sphere obstacles (15% solid)
-  channel   REFERENCE semantics, periodic x, walls up/down (plbpd's own
-            operator sequence, bit-exact with the reference)
+  channel   REFERENCE semantics, periodic x (and y in 3D), walls up/down
+            (plbpd's own operator sequence, bit-exact with the reference)
 --nx/--ny/--nz override --n per axis.  Used for quick measurements and for
 small profiler captures.
 """
@@ -56,7 +56,11 @@ def params_for(a):
         return capi.make_params(a.model, nx, ny, nz, nu, force=(a.force, 0.0, 0.0), face_type=faces, face_vel=vel,
                                 semantics=capi.SEMANTICS_NATIVE, arith=ar, storage=st, **col)
     if a.workload == "channel":
+        # walls up and down, periodic x (and y: a face left out would be open,
+        # and an open face loses mass until the flow fails)
         faces = {"east": "periodic", "west": "periodic", "up": "noslip", "down": "noslip"}
+        if a.model != "D2Q9":
+            faces.update(north="periodic", south="periodic")
         vel = {"up": (0.0, 0.0, 0.0), "down": (0.0, 0.0, 0.0)}
         return capi.make_params(a.model, nx, ny, nz, nu, force=(a.force, 0.0, 0.0), face_type=faces, face_vel=vel,
                                 semantics=capi.SEMANTICS_REFERENCE, arith=ar, **col)
