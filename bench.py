@@ -274,7 +274,7 @@ KERNELS = {("reference", "fp32", 0): "nat_fused_k<19,fp32,nomask,reference> (one
            ("fp32", "fp32", 2): "nat_fused_h2_k<19,fp32,nomask,form 1> (two nodes a thread, paired FP32)",
            ("fp32", "fp32", 3): "nat_fused_h2_k<19,fp32,nomask,form 2> (two nodes a thread, scalar update)"}
 TRAFFIC = {("reference", "fp32", 0): (2495973034, "profiles/nat_fused_ref_d3q19_256.md"),
-           ("reference", "fp32", 1): (2493956864, "profiles/nat_fused_h2_ref_d3q19_256.md"),
+           ("reference", "fp32", 1): (2491876522, "profiles/nat_fused_h2_ref_d3q19_256.md"),
            ("fp32", "fp32", 0): (2495234680, "profiles/nat_fused_d3q19_256.md"),
            ("fp32", "fp32", 1): (2494710954, "profiles/nat_fused_d3q19_256.md"),
            ("fp32", "fp32", 2): (2494610944, "profiles/nat_fused_d3q19_256.md"),
