@@ -191,6 +191,13 @@ __global__ void ref_noslip_k(Geo g, FaceParams fp, int f0, int f1, int nfaces,
     if (a >= na || b >= nb) return;
     const float* ub = fp.vel[face];
     const long long A = g.idx(x, y, z);
+    // every value this thread reads first: its stores go to slots no later
+    // read of this thread (or of another thread, see above) touches, and
+    // with the reads in between the compiler would have to keep each read
+    // after the previous store (18 round trips in a row for D3Q19)
+    float nA[Q];
+#pragma unroll
+    for (int kp = 1; kp < Q; ++kp) nA[kp] = n[rev_of(kp) * g.ks + A];
 #pragma unroll
     for (int kp = 1; kp < Q; ++kp) {
         const int k = rev_of(kp);
@@ -204,14 +211,14 @@ __global__ void ref_noslip_k(Geo g, FaceParams fp, int f0, int f1, int nfaces,
             // A (first) writes (B, kp) from the original (A, k); B then writes
             // (A, k) from the value A just wrote.
             const float t1 = wall_term<Q>(k, rho[B], dot_c_full<Q>(k, ub), fp.cs2inv);
-            const float vB = __fsub_rn(n[k * g.ks + A], t1);
+            const float vB = __fsub_rn(nA[kp], t1);
             const float t2 = wall_term<Q>(kp, rho[A], dot_c_full<Q>(kp, ub), fp.cs2inv);
             const float vA = __fsub_rn(vB, t2);
             n[kp * g.ks + B] = vB;
             n[k * g.ks + A] = vA;
         } else {
             const float t = wall_term<Q>(k, rho[B], dot_c_full<Q>(k, ub), fp.cs2inv);
-            n[kp * g.ks + B] = __fsub_rn(n[k * g.ks + A], t);
+            n[kp * g.ks + B] = __fsub_rn(nA[kp], t);
         }
     }
 }
@@ -227,26 +234,35 @@ __global__ void ref_periodic_k(Geo g, FaceParams fp, float* __restrict__ n) {
     const int z = blockIdx.y;
     const int n_ew = fp.ew_periodic ? g.ny : 0;
     const int n_ns = fp.ns_periodic ? g.nx : 0;
+    // a thread reads halo slots and writes interior ones, so all its reads
+    // go first (with a store between two reads the compiler keeps them in
+    // order: one round trip after another)
+    float v[Q];
     if (t < n_ew) {
         const int y = t;
 #pragma unroll
         for (int k = 1; k < Q; ++k) {
+            const int cx = Lattice<Q>::cx(k);
+            if (cx != 0) v[k] = n[k * g.ks + g.idx(cx > 0 ? g.nx : -1, y, z)];
+        }
+#pragma unroll
+        for (int k = 1; k < Q; ++k) {
             const int cx = Lattice<Q>::cx(k), cy = Lattice<Q>::cy(k);
             if (cx == 0) continue;
-            const int xd = cx > 0 ? 0 : g.nx - 1;
-            const int xs = cx > 0 ? g.nx : -1;
             if (fp.ns_periodic && ((cy > 0 && y == 0) || (cy < 0 && y == g.ny - 1))) continue;
-            n[k * g.ks + g.idx(xd, y, z)] = n[k * g.ks + g.idx(xs, y, z)];
+            n[k * g.ks + g.idx(cx > 0 ? 0 : g.nx - 1, y, z)] = v[k];
         }
     } else if (t < n_ew + n_ns) {
         const int x = t - n_ew;
 #pragma unroll
         for (int k = 1; k < Q; ++k) {
             const int cy = Lattice<Q>::cy(k);
-            if (cy == 0) continue;
-            const int yd = cy > 0 ? 0 : g.ny - 1;
-            const int ysrc = cy > 0 ? g.ny : -1;
-            n[k * g.ks + g.idx(x, yd, z)] = n[k * g.ks + g.idx(x, ysrc, z)];
+            if (cy != 0) v[k] = n[k * g.ks + g.idx(x, cy > 0 ? g.ny : -1, z)];
+        }
+#pragma unroll
+        for (int k = 1; k < Q; ++k) {
+            const int cy = Lattice<Q>::cy(k);
+            if (cy != 0) n[k * g.ks + g.idx(x, cy > 0 ? 0 : g.ny - 1, z)] = v[k];
         }
     }
 }
