@@ -205,3 +205,28 @@ def test_pinned_host_buffers_transfer_directly(storage):
             t.set(capi.FIELD_N, n)
             assert_bitexact(got, t.get(capi.FIELD_N), "set n")
         pn.free()
+
+
+@pytest.mark.parametrize("case", ["obstacles_d3q19", "torus_d3q27", "channel_d2q9"])
+def test_moments_read_without_populations(case):
+    """rho and u read straight after a march (a gather of the moments alone,
+    no population read first) equal the oracle's, and a later read of n still
+    does."""
+    from plbpd_gb300 import capi
+    cfg = NATIVE_CASES[case]
+    mask = mask_for(case, cfg)
+    p = po.Port(**cfg, mode=po.MODE_NATIVE, mask=mask, arith=po.ARITH_FP32)
+    p._cfg = cfg
+    p.initialize()
+    n, rho, u = perturbed_start(p, 5)
+    p.set(po.N, n); p.set(po.RHO, rho); p.set(po.U, u)
+    p.step(23)
+    with capi.Solve.create(**cfg, semantics=capi.SEMANTICS_NATIVE, arith=capi.ARITH_FP32) as s:
+        if mask is not None:
+            s.set_mask(mask)
+        s.initialize()
+        s.set(0, n); s.set(2, rho); s.set(3, u)
+        s.step(23)
+        assert_bitexact(s.get(3)[1:-1, 1:-1, 1:-1], p.get(po.U)[1:-1, 1:-1, 1:-1], f"{case} u first")
+        assert_bitexact(s.get(2)[1:-1, 1:-1, 1:-1], p.get(po.RHO)[1:-1, 1:-1, 1:-1], f"{case} rho")
+        compare(s, p, mask, f"{case} after the moment reads")
